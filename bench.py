@@ -1,0 +1,282 @@
+#!/usr/bin/env python3
+"""AMG-PCG benchmark: DOF/s to 1e-8 relative residual on one GB300.
+
+Workload (one "step" = one pass of the hot path): AMG setup (OldMIS aggregation,
+smoothed prolongator, Galerkin RAP) + flexible PCG to ||r||/||b|| <= 1e-8 on the
+3D Poisson problem on the unit cube, 128^3 cells Kuhn-split into 12,582,912 P1
+tets (2,146,689 vertices), kappa_e = exp(2 g_e), g ~ N(0,1) (seed 4), f ~ U[-1,1]
+(seed 5), u = 0 on z = 0.  value = free DOF x steps / device time (inputs in HBM);
+e2e = the same through femgpu_setup + femgpu_solve with host b/x buffers.
+
+--precision mixed (default): FP32 hierarchy inside the FP64 outer PCG;
+--precision fp64: the same code with an FP64 hierarchy.
+--impl reference: the reference algorithm's CPU restatement (oracle) on host cores.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "sci-solver_fem_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "AMG-PCG DOF/s to 1e-8 rel-resid, mixed vs FP64 on 1 GB300; SpMV HBM GB/s"
+UNIT = "DOF/s"
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def problem(n, sigma):
+    from femgpu import meshes
+    return meshes.poisson3d_problem(n, sigma=sigma, kappa_seed=4, f_seed=5)
+
+
+def cpu_baseline(n_sample, sigma, threads):
+    """The reference algorithm restated on the CPU (oracle), timed on host cores."""
+    import oracle as O
+    from femgpu import meshes
+    xyz, conn, kappa, f, mask = problem(n_sample, sigma)
+    rp, ci = O.build_pattern(xyz.shape[0], conn)
+    v = O.assemble(xyz, conn, rp, ci, coef=kappa, lambda_mass=0.0)
+    b = O.load_vector(xyz, conn, f)
+    v, b = O.apply_dirichlet(rp, ci, v, mask, b)
+    gx, ga = meshes.adjacency_from_pattern(rp, ci)
+    t0 = time.perf_counter()
+    amg = O.OracleAMG(rp, ci, v, gx, ga, seed=1, threads=threads)
+    x, st = amg.pcg(b, tol=1e-8, max_iters=500, flexible=True)
+    dt = time.perf_counter() - t0
+    free = int(xyz.shape[0] - mask.sum())
+    return free / dt, dt, st
+
+
+def run_reference(args):
+    """--impl reference: the reference's algorithm on the host cores (oracle port)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = len(os.sched_getaffinity(0))
+    n_sample = args.cpu_sample
+    for _ in range(args.warmup):
+        cpu_baseline(n_sample, args.sigma, threads)
+    vals, times = [], []
+    for _ in range(args.steps):
+        v, dt, st = cpu_baseline(n_sample, args.sigma, threads)
+        vals.append(v)
+        times.append(dt)
+    value = float(np.mean(vals))
+    sample = (f"{n_sample}^3-cell Kuhn tet sample of the same Poisson problem family "
+              f"({(n_sample + 1) ** 3} vertices), setup + PCG to 1e-8 per step")
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(times)),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic", "config": {"workload": f"poisson3d_kuhn_{args.n}^3_sigma{args.sigma:g}",
+                                           "parallelism": "host cores"},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=128, help="cells per cube edge")
+    ap.add_argument("--sigma", type=float, default=2.0)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--cpu-sample", type=int, default=48)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+    import femgpu
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    # ---- problem (replicas only: each rank solves its own copy) -------------------
+    xyz, conn, kappa, f, mask = problem(args.n, args.sigma)
+    n = xyz.shape[0]
+    free = int(n - mask.sum())
+    stream = torch.cuda.Stream()  # the solver and every torch op below share this stream
+    torch.cuda.set_stream(stream)
+    prec = 0 if args.precision == "mixed" else 1
+    s = femgpu.Solver(solverType=1, tolerance=1e-8, maxIters=500, flexibleCG=1, seed=1, precision=prec,
+                      device=local, stream=stream.cuda_stream)
+    t_asm0 = time.perf_counter()
+    s.set_mesh(xyz, conn)
+    s.assemble(kappa, 0.0)
+    b = s.load_vector(f)
+    s.set_dirichlet(mask)
+    b[mask.astype(bool)] = 0.0
+    torch.cuda.synchronize()
+    assembly_ms = 1e3 * (time.perf_counter() - t_asm0)
+
+    d_b = torch.from_numpy(b).cuda()
+    d_x = torch.zeros(n, dtype=torch.float64, device="cuda")
+
+    def step():
+        s.setup()
+        d_x.zero_()
+        return s.solve_device(d_b.data_ptr(), d_x.data_ptr())
+
+    for _ in range(args.warmup):
+        st = step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = femgpu.kernel_launches()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    iters, setup_ms, solve_ms = [], [], []
+    for _ in range(args.steps):
+        st = step()
+        iters.append(st["iterations"])
+        setup_ms.append(st["setup_ms"])
+        solve_ms.append(st["solve_ms"])
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    launches = femgpu.kernel_launches() - launches0
+    ms = e0.elapsed_time(e1) / args.steps
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    relres = st["relres"]
+    value = world * free / (ms / 1e3)
+
+    # ---- end to end through the C ABI with host buffers ---------------------------
+    x_h = np.zeros(n)
+    b_h = b.copy()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s.setup()
+        x_h[:] = 0.0
+        x_h, st2 = s.solve(b_h, x_h)
+    e2e_ms = 1e3 * (time.perf_counter() - t0) / args.steps
+    e2e = {"value": world * free / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": 16 * n,
+           "d2h_bytes_per_step": 8 * n}
+    clk = clocks.stop()
+
+    # ---- roofline: FP64 CSR SpMV of the outer PCG (CUDA events on the solver's stream)
+    peak, peak_kind = peaks()
+    rp, ci, _ = s.matrix()
+    nnz = int(ci.shape[0])
+    y = torch.empty_like(d_x)
+    for _ in range(3):
+        s.spmv_device(d_x.data_ptr(), y.data_ptr())
+    reps = 20
+    a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a0.record(stream)
+    for _ in range(reps):
+        s.spmv_device(d_x.data_ptr(), y.data_ptr())
+    a1.record(stream)
+    torch.cuda.synchronize()
+    spmv_ms = a0.elapsed_time(a1) / reps
+    spmv_bytes = 12 * nnz + 4 * (n + 1) + 8 * n + 8 * n
+    achieved = spmv_bytes / (spmv_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": "spmv_kernel (FP64 CSR, outer PCG)", "achieved": round(achieved, 1),
+                "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                "peak_source": peak_kind, "algorithmic_bytes": spmv_bytes, "ms": round(spmv_ms, 4)}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = len(os.sched_getaffinity(0))
+        v, dt, _ = cpu_baseline(args.cpu_sample, args.sigma, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{args.cpu_sample}^3-cell Kuhn sample of the same problem ({(args.cpu_sample + 1) ** 3} "
+                         f"vertices), oracle setup + PCG to 1e-8, {dt:.1f} s"}
+
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f64+f32" if prec == 0 else "f64", "data": "synthetic",
+               "config": {"workload": f"poisson3d_kuhn_{args.n}^3_sigma{args.sigma:g}", "dofs": n,
+                          "free_dofs": free, "elements": int(conn.shape[0]), "nnz": nnz,
+                          "precision": args.precision, "tolerance": 1e-8, "parallelism": "replicas" if world > 1 else "1 GPU",
+                          "l2": "inputs larger than L2 (A: %.0f MB)" % (12 * nnz / 1e6)},
+               "pcg_iterations": iters[-1], "relres": relres, "setup_ms": float(np.mean(setup_ms)),
+               "solve_ms": float(np.mean(solve_ms)), "assembly_ms": assembly_ms,
+               "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu,
+               "clocks": clk}
+        print(json.dumps(out))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,186 @@
+/*
+ * femgpu.h -- C ABI of the GB300-native P1 FEM -> smoothed-aggregation AMG -> PCG
+ * solver.  Plain pointers and sizes only; every call returns a status code and
+ * never exits the process.
+ *
+ * The reference exposes this path as the C++ class FEMSolver (src/FEMSolver.h:14-67
+ * of SCI-Solver_FEM).  The C++ drop-in (include/FEMSolver.h) is a thin layer over
+ * these entry points; foreign-language bindings (ctypes, cgo, JNI) call them
+ * directly.  Each declaration names the reference interface it replaces.
+ *
+ * Ownership: the caller owns every host buffer and the library copies on entry;
+ * device memory belongs to the handle and is released by femgpu_destroy.  All
+ * device work runs on the handle's stream (config.stream, NULL = a private stream).
+ * Calls on one handle must not overlap; distinct handles are independent.
+ */
+#ifndef FEMGPU_H
+#define FEMGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  FEMGPU_OK = 0,
+  FEMGPU_ERR_INVALID = 1,        /* bad argument or call order */
+  FEMGPU_ERR_CUDA = 2,           /* CUDA runtime error */
+  FEMGPU_ERR_NOT_READY = 3,      /* mesh / matrix / hierarchy missing */
+  FEMGPU_ERR_BREAKDOWN = 4,      /* PCG breakdown (non-positive p'Ap, NaN/Inf), singular coarse matrix */
+  FEMGPU_ERR_NOT_CONVERGED = 5,  /* max iterations reached */
+  FEMGPU_ERR_LIMIT = 6,          /* a bounded loop or a size limit was hit */
+  FEMGPU_ERR_IO = 7,             /* file could not be read / parsed */
+  FEMGPU_ERR_ALLOC = 8,          /* device allocation failed */
+  FEMGPU_ERR_NO_DEVICE = 9       /* no CUDA device visible */
+} femgpu_status;
+
+typedef struct femgpu_ctx* femgpu_handle;
+
+/* Solver options.  The first block mirrors the public members of the reference's
+ * FEMSolver (src/FEMSolver.h:37-56) with the same defaults (src/FEMSolver.cu:9-35). */
+typedef struct {
+  int verbose;              /* verbose_            0 */
+  int maxLevels;            /* maxLevels_          100 */
+  int maxIters;             /* maxIters_           100 */
+  int preInnerIters;        /* preInnerIters_      5 */
+  int postInnerIters;       /* postInnerIters_     5 */
+  int postRelaxes;          /* postRelaxes_        1 */
+  int cycleIters;           /* cycleIters_         1 */
+  int dsType;               /* dsType_             0 (only the symmetric split is built) */
+  int topSize;              /* topSize_            256 */
+  int randMisParameters;    /* randMisParameters_  90102 */
+  int partitionMaxSize;     /* partitionMaxSize_   512 */
+  int aggregatorType;       /* aggregatorType_     0 (OldMIS; others rejected) */
+  int convergeType;         /* convergeType_       0 (the PCG test is relative, as in the reference) */
+  double tolerance;         /* tolerance_          1e-6 */
+  int cycleType;            /* cycleType_          0 (V) */
+  int solverType;           /* solverType_         0 = one V-cycle, 1 = PCG */
+  double smootherWeight;    /* smootherWeight_     1.0 */
+  double proOmega;          /* proOmega_           0.67 */
+  int device;               /* device_             0 */
+  int blockSize;            /* blockSize_          256 */
+  /* Additions (no counterpart in the reference). */
+  uint32_t seed;            /* replaces srand(time(NULL)) in the MIS: 1 */
+  int precision;            /* 0 = FP32 hierarchy in an FP64 outer PCG (reference), 1 = FP64 hierarchy */
+  int flexibleCG;           /* 0 = Fletcher-Reeves beta (reference), 1 = Polak-Ribiere (flexible) */
+  void* stream;             /* cudaStream_t to run on; NULL = library-owned stream */
+} femgpu_config;
+
+typedef struct {
+  int iterations;           /* PCG iterations (SpMVs) performed */
+  double relative_residual; /* ||b - A x|| / ||b|| at exit */
+  double setup_ms;          /* last femgpu_setup: hierarchy build */
+  double solve_ms;          /* last solve: device time */
+  int num_levels;
+} femgpu_solve_stats;
+
+/* Per-level statistics (AMG::printGridStatistics, src/core/cuda/amg.cu:202-231). */
+typedef struct {
+  int64_t rows, nnz, aggregates, partitions, nnz_p;
+} femgpu_level_info;
+
+/* Defaults of the FEMSolver constructor (src/FEMSolver.cu:9-35). */
+void femgpu_config_default(femgpu_config* cfg);
+
+/* Creates a solver context on cfg->device.  Replaces FEMSolver::InitCUDA
+ * (src/FEMSolver.cu:99-129), which the reference never calls. */
+femgpu_status femgpu_create(femgpu_handle* h, const femgpu_config* cfg);
+femgpu_status femgpu_destroy(femgpu_handle h);
+const char* femgpu_status_string(femgpu_status s);
+/* Last error message recorded on this handle (empty string if none). */
+const char* femgpu_last_error(femgpu_handle h);
+
+/* Sets the mesh and builds the CSR sparsity pattern on the device.
+ * dim = 3: tetrahedra (nodes_per_elem = 4); dim = 2: triangles (3).
+ * xyz: nverts x 3 doubles (z ignored for dim 2); conn: nelems x nodes_per_elem
+ * 0-based vertex ids; labels: per-element material labels or NULL.
+ * Replaces TetMesh::read / TriMesh::read + need_neighbors + tetmesh2ell /
+ * trimesh2ell (src/core/cuda/tetmesh.cu:112-170,251-376; cutil.cu:168-230,297-348). */
+femgpu_status femgpu_set_mesh(femgpu_handle h, int dim, int64_t nverts, const double* xyz,
+                              int64_t nelems, const int32_t* conn, const int32_t* labels);
+
+/* Assembles A = sum_e c_e K_e + lambda_mass M_e into the pattern.  coef (per
+ * element, host) gives c_e; when coef is NULL, c_e comes from the labels
+ * (1,1,2,3,4,5,6 for labels 0..6) in 3D and is 1 in 2D.  Replaces
+ * FEM3D::assemble / FEM2D::assemble + element_loop_3d_kernel / element_loop_kernel
+ * (src/core/cuda/FEM3D.cu:501-557; perform_element_loop_3D.cuh:480-627;
+ * FEM2D.cu:358-378; perform_element_loop_2D.cuh:287-372); the reference fixes
+ * lambda_mass = 1 and coef = NULL. */
+femgpu_status femgpu_assemble(femgpu_handle h, const double* coef, double lambda_mass);
+
+/* Load vector b = M f (consistent P1 mass) for nodal f (host arrays, nverts).
+ * No reference counterpart: its force function is 0 (perform_element_loop_3D.cuh:22-26). */
+femgpu_status femgpu_load_vector(femgpu_handle h, const double* f, double* b);
+
+/* Symmetric Dirichlet elimination u = 0 on mask[i] != 0: rows and columns zeroed,
+ * unit diagonal.  No reference counterpart (the reference applies no BC). */
+femgpu_status femgpu_set_dirichlet(femgpu_handle h, const uint8_t* mask);
+
+/* Replaces the operator with a host CSR matrix (sorted columns); the level-0
+ * aggregation graph stays the mesh graph when a mesh is set, else it is the
+ * matrix pattern.  Replaces the MAT-override path of
+ * FEMSolver::readMatlabSparseMatrix (src/FEMSolver.cu:177-356). */
+femgpu_status femgpu_set_matrix_csr(femgpu_handle h, int64_t n, const int32_t* rowptr,
+                                    const int32_t* cols, const double* vals);
+
+/* Builds the AMG hierarchy for the current operator.  Replaces AMG::setup
+ * (src/core/cuda/amg.cu:80-144) with createNextLevel / OldMIS / RAP. */
+femgpu_status femgpu_setup(femgpu_handle h);
+
+/* Solves A x = b.  x holds the initial guess on entry (host arrays, n doubles).
+ * solverType 0: one V-cycle; 1: PCG to tolerance.  Replaces FEMSolver::solveFEM
+ * (src/FEMSolver.cu:58-93) -> AMG::solve (amg.cu:174-200) -> CG_Flex_Cycle
+ * (cgcycle.cu:6-69).  stats may be NULL. */
+femgpu_status femgpu_solve(femgpu_handle h, const double* b, double* x, femgpu_solve_stats* stats);
+
+/* Same as femgpu_solve with device pointers on the handle's stream (no copies). */
+femgpu_status femgpu_solve_device(femgpu_handle h, const double* d_b, double* d_x,
+                                  femgpu_solve_stats* stats);
+
+/* y = A x with the level-0 FP64 operator, device pointers, original numbering.
+ * Replaces cusp::multiply(Ahyb_d_CG, ...) in cgcycle.cu:24,38. */
+femgpu_status femgpu_spmv_device(femgpu_handle h, const double* d_x, double* d_y);
+
+/* ---- inspection (parity tests, statistics) --------------------------------- */
+/* Pattern/values of the assembled level-0 matrix (original numbering). Any
+ * output pointer may be NULL; n and nnz are always written. */
+femgpu_status femgpu_get_matrix(femgpu_handle h, int64_t* n, int64_t* nnz, int32_t* rowptr,
+                                int32_t* cols, double* vals);
+/* Number of levels of the current hierarchy (AMG::num_levels). */
+femgpu_status femgpu_num_levels(femgpu_handle h, int* levels);
+femgpu_status femgpu_get_level_info(femgpu_handle h, int level, femgpu_level_info* info);
+/* Level arrays: A (level's own numbering, values as double), the permutation
+ * (old -> new), aggregate and partition offsets (SmoothedMG_AMG_Level members
+ * permutation_d / aggregateIdx_d / partitionIdx_d) and P.  NULL skips an array. */
+femgpu_status femgpu_level_get(femgpu_handle h, int level, int32_t* A_rowptr, int32_t* A_cols,
+                               double* A_vals, int32_t* perm, int32_t* agg_idx, int32_t* part_idx,
+                               int32_t* P_rowptr, int32_t* P_cols, double* P_vals);
+/* One V-cycle z = M r on host vectors (AMG_Level::cycle_level0, amg_level.cu:74-128). */
+femgpu_status femgpu_vcycle(femgpu_handle h, const double* r, double* z);
+/* Number of kernel launches issued by the library on this handle so far. */
+femgpu_status femgpu_kernel_launches(femgpu_handle h, int64_t* count);
+
+/* ---- file IO (host) ---------------------------------------------------------- */
+/* Reads .node/.ele (TetMesh::read, tetmesh.cu:251-376) or ASCII/binary-LE PLY
+ * (TriMesh::read, TriMesh_io.cu:146-257).  Two-call protocol: with NULL arrays
+ * only the counts are returned.  Coordinates are parsed as float, as the reference. */
+femgpu_status femgpu_read_tetgen(const char* node_file, const char* ele_file, int64_t* nverts,
+                                 int64_t* nelems, double* xyz, int32_t* conn, int32_t* labels);
+femgpu_status femgpu_read_ply(const char* file, int64_t* nverts, int64_t* nfaces, double* xyz,
+                              int32_t* conn);
+/* MAT v5 (uncompressed) sparse matrix / double array, FEMSolver::readMatlabSparseMatrix /
+ * readMatlabArray (src/FEMSolver.cu:177-449).  Sparse output is CSR with sorted columns. */
+femgpu_status femgpu_read_mat_sparse(const char* file, int64_t* rows, int64_t* cols, int64_t* nnz,
+                                     int32_t* rowptr, int32_t* colidx, double* vals);
+femgpu_status femgpu_read_mat_array(const char* file, int64_t* n, double* vals);
+/* FEMSolver::writeMatlabArray / writeVTK (src/FEMSolver.cu:451-582). */
+femgpu_status femgpu_write_mat_array(const char* file, int64_t n, const double* vals);
+femgpu_status femgpu_write_vtk(const char* file, int dim, int64_t nverts, const double* xyz,
+                               int64_t nelems, const int32_t* conn, const double* values);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FEMGPU_H */

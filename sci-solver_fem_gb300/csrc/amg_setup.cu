@@ -1,0 +1,1181 @@
+// amg_setup.cu -- smoothed-aggregation hierarchy built on the device.
+//
+// Per level (AMG::setup, src/core/cuda/amg.cu:80-144; createNextLevel,
+// smoothedMG_amg_level.cu:403-494):
+//   1. OldMIS two-level aggregation of the level graph (ComputePermutationMethods.cu:22-151):
+//      seeded distance-2 randomized MIS -> aggregates (min size 9) -> distance-1 MIS on
+//      the aggregate graph -> partitions of <= partitionMaxSize rows;
+//   2. the permutation that makes aggregates and partitions contiguous;
+//   3. Ap = perm(A), the in/out-of-partition split used by the smoother;
+//   4. P = (I - omega D^-1 Ap) T, R = P^T;
+//   5. A_next = R (Ap P) by a row-wise expand-sort-compress SpGEMM in shared memory.
+// Integer results are bit-identical to the CPU oracle for the same seed; floating
+// results use fixed summation orders (see row_esc_kernel).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+
+#include "context.cuh"
+
+namespace femgpu {
+
+namespace {
+
+constexpr int kCap = 100000;  // bound on every data-dependent loop (error, never spin)
+
+// ---------------------------------------------------------------------------------
+// glibc rand() stream (TYPE_3 additive feedback generator), host side: the
+// reference draws 32768 seeds with rand() after srand() (randomizedMIS_GPU.cu:195-201).
+void glibc_rand_stream(uint32_t seed, int count, std::vector<uint32_t>& out) {
+  std::vector<uint32_t> st(344 + (size_t)count);
+  int32_t s0 = (int32_t)(seed ? seed : 1u);
+  st[0] = (uint32_t)s0;
+  int64_t w = s0;
+  for (int i = 1; i < 31; i++) {
+    w = (16807LL * w) % 2147483647LL;
+    if (w < 0) w += 2147483647LL;
+    st[i] = (uint32_t)w;
+  }
+  for (int i = 31; i < 34; i++) st[i] = st[i - 31];
+  for (size_t i = 34; i < st.size(); i++) st[i] = st[i - 31] + st[i - 3];
+  out.resize(count);
+  for (int k = 0; k < count; k++) out[k] = st[344 + (size_t)k] >> 1;
+}
+
+__device__ __forceinline__ uint32_t taus(uint32_t z) {
+  uint32_t b = (((z << 13) ^ z) >> 19);
+  return (z << 12) ^ b;
+}
+
+// ---- randomized MIS (randomizedMIS_GPU.cu:3-152) ---------------------------------
+__global__ void mis_randoms_kernel(int n, int iterations, uint32_t* randoms, const uint32_t* seeds) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 32768) return;
+  uint32_t z = seeds[t];
+  int off = t;
+  for (int i = 0; i < iterations; i++)
+    if (off < n) {
+      z = taus(z);
+      randoms[off] = z;
+      off += 32768;
+    }
+}
+
+__global__ void mis_first_init_kernel(int n, const uint32_t* randoms, int32_t* best, int32_t* origin) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    origin[i] = i;
+    best[i] = (int32_t)(randoms[i] % 1000000u);
+  }
+}
+
+__global__ void mis_init_kernel(int n, uint32_t* randoms, int32_t* best, int32_t* origin, const int32_t* mis) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    uint32_t z = taus(randoms[i]);
+    origin[i] = i;
+    int st = mis[i];
+    best[i] = st == -1 ? (int32_t)(z % 1000000u) : (st == 1 ? 1000001 : 0);
+    randoms[i] = z;
+  }
+}
+
+__global__ void mis_iterate_kernel(int n, const int32_t* __restrict__ oin, int32_t* __restrict__ oout,
+                                   const int32_t* __restrict__ bin, int32_t* __restrict__ bout,
+                                   const int32_t* __restrict__ xadj, const int32_t* __restrict__ adj, int32_t* mis,
+                                   int32_t* incomplete, int final_pass) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int best = bin[i], org = oin[i];
+  if (best < 1000001) {
+    for (int e = xadj[i]; e < xadj[i + 1]; e++) {
+      int nb = adj[e];
+      int ch = bin[nb], cho = oin[nb];
+      if (ch > 0 && ch == best && cho > org) org = cho;
+      if (ch > best) {
+        best = ch;
+        org = cho;
+      }
+    }
+  }
+  bout[i] = best;
+  oout[i] = org;
+  if (final_pass) {
+    int st = -1;
+    if (org == i) st = 1;
+    else if (best == 1000001) st = 0;
+    mis[i] = st;
+    if (st == -1) *incomplete = 1;
+  }
+}
+
+void random_mis(Ctx& c, int n, const int32_t* xadj, const int32_t* adj, int k, DBuf<int32_t>& mis) {
+  cudaStream_t s = c.stream;
+  mis.alloc(n, s);
+  fill_i32(mis.p, n, -1, s);
+  std::vector<uint32_t> seeds;
+  glibc_rand_stream(c.cfg.seed, 32768, seeds);
+  DBuf<uint32_t> dseeds(32768, s), randoms(n, s);
+  dseeds.upload(seeds.data(), 32768);
+  DBuf<int32_t> b0(n, s), b1(n, s), o0(n, s), o1(n, s), flag(1, s);
+  FG_LAUNCH(mis_randoms_kernel, 128, 256, 0, s, n, (n + 32767) / 32768, randoms.p, dseeds.p);
+  FG_LAUNCH(mis_first_init_kernel, grid_for(n, 256), 256, 0, s, n, randoms.p, b0.p, o0.p);
+  for (int round = 0;; round++) {
+    FG_REQUIRE(round < kCap, FEMGPU_ERR_LIMIT, "randomized MIS did not complete");
+    if (round > 0) FG_LAUNCH(mis_init_kernel, grid_for(n, 256), 256, 0, s, n, randoms.p, b0.p, o0.p, mis.p);
+    flag.zero();
+    int32_t *bi = b0.p, *bo = b1.p, *oi = o0.p, *oo = o1.p;
+    for (int it = 0; it < k; it++) {
+      FG_LAUNCH(mis_iterate_kernel, grid_for(n, 256), 256, 0, s, n, oi, oo, bi, bo, xadj, adj, mis.p, flag.p,
+                it == k - 1);
+      std::swap(bi, bo);
+      std::swap(oi, oo);
+    }
+    if (bi != b0.p) {  // keep b0/o0 as the next round's input buffers
+      std::swap(b0.p, b1.p);
+      std::swap(o0.p, o1.p);
+    }
+    if (read_scalar(flag.p, s) == 0) break;
+  }
+}
+
+// ---- aggregation helpers (misHelpers.cu) ----------------------------------------------
+__global__ void label_roots_kernel(int n, const int32_t* mis, const int32_t* incl, int32_t* part, int32_t* aggregated) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    aggregated[i] = mis[i];
+    part[i] = mis[i] == 0 ? -1 : incl[i] - 1;  // ifLabelOne
+  }
+}
+
+// allocateNodesKernel (misHelpers.cu:13-75): its candidate loop fills every free slot
+// with the first aggregated neighbour seen and can never out-count it, so an
+// unaggregated node joins the aggregate of its first aggregated neighbour in
+// adjacency order.  Writes the full partOut so the buffers can be swapped.
+__global__ void allocate_kernel(int n, const int32_t* __restrict__ xadj, const int32_t* __restrict__ adj,
+                                const int32_t* __restrict__ pin, int32_t* __restrict__ pout, int32_t* aggregated,
+                                int32_t* counters /* [0] unallocated after, [1] changed */) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int p = pin[i];
+  if (aggregated[i] == 0) {
+    int add = -1;
+    for (int e = xadj[i]; e < xadj[i + 1]; e++) {
+      int cnd = pin[adj[e]];
+      if (cnd != -1) {
+        add = cnd;
+        break;
+      }
+    }
+    p = add;
+    if (add != -1) {
+      aggregated[i] = 1;
+      atomicExch(&counters[1], 1);
+    } else {
+      atomicAdd(&counters[0], 1);
+    }
+  }
+  pout[i] = p;
+}
+
+__global__ void histogram_kernel(int n, const int32_t* part, const int32_t* w, int32_t* sizes) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    int p = part[i];
+    if (p >= 0) atomicAdd(&sizes[p], w ? w[i] : 1);
+  }
+}
+
+__global__ void less_than_kernel(int np, const int32_t* sizes, int threshold, int32_t* flags) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < np) flags[p] = sizes[p] < threshold ? 1 : 0;
+}
+
+__global__ void remove_parts_kernel(int n, int32_t* part, const int32_t* rm, const int32_t* sub, int32_t* aggregated) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    int p = part[i];
+    int q = rm[p] ? -1 : p - sub[p];
+    part[i] = q;
+    aggregated[i] = q == -1 ? 0 : 1;
+  }
+}
+
+// findDesirabilityKernel (misHelpers.cu:297-382) with IEEE float steps spelled out.
+__global__ void desirability_kernel(int n, int opt, const int32_t* __restrict__ xadj, const int32_t* __restrict__ adj,
+                                    const int32_t* __restrict__ part, const int32_t* __restrict__ sizes,
+                                    const int32_t* __restrict__ w, int32_t* to,
+                                    unsigned long long* best /* per partition: (desirability bits, node) */) {
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n) return;
+  int cur = part[idx];
+  int cs = sizes[cur];
+  int nw = w[idx];
+  int selfAdj = 0, addTo = -1;
+  float bestD = 0.0f;
+  float cwf = __fdiv_rn((float)abs(cs - opt), (float)opt);
+  float selfImp = __fmul_rn((float)(abs(cs - opt) - abs((cs - nw) - opt)), cwf);
+  if (selfImp > 0) {
+    int cand[10], cnt[10];
+#pragma unroll
+    for (int q = 0; q < 10; q++) {
+      cand[q] = -1;
+      cnt[q] = 0;
+    }
+    for (int e = xadj[idx]; e < xadj[idx + 1]; e++) {
+      int cc = part[adj[e]];
+      if (cc == cur) {
+        selfAdj++;
+        continue;
+      }
+      // distinct candidates in first-seen order, at most 10 (junk counts of free
+      // slots in the reference never reach a used slot)
+#pragma unroll
+      for (int q = 0; q < 10; q++) {
+        if (cand[q] == cc) {
+          cnt[q]++;
+          break;
+        }
+        if (cand[q] == -1) {
+          cand[q] = cc;
+          cnt[q] = 1;
+          break;
+        }
+      }
+    }
+    // the reference scans candidates 1..9 (its loop starts at 1)
+#pragma unroll
+    for (int q = 1; q < 10; q++) {
+      if (cand[q] == -1) continue;
+      int np_ = cand[q];
+      int nsz = sizes[np_];
+      float nwf = __fdiv_rn((float)abs(nsz - opt), (float)opt);
+      float imp = __fmul_rn((float)(abs(nsz - opt) - abs((nsz + nw) - opt)), nwf);
+      imp = __fadd_rn(imp, selfImp);
+      float ratio = __fdiv_rn((float)cnt[q], (float)selfAdj);
+      imp = __fmul_rn(imp, ratio);
+      if (imp > bestD) {
+        addTo = np_;
+        bestD = imp;
+      }
+    }
+  }
+  to[idx] = addTo;
+  unsigned long long key = ((unsigned long long)__float_as_uint(bestD) << 32) | (unsigned)idx;
+  atomicMax(&best[cur], key);
+}
+
+// makeSwapsKernel (misHelpers.cu:384-412): per source partition, the node with the
+// largest (desirability, index) moves when its desirability exceeds 0.1.
+__global__ void swap_kernel(int np, unsigned long long* best, int32_t* part, const int32_t* to, const int32_t* w,
+                            int32_t* sizes) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  unsigned long long key = best[p];
+  best[p] = 0ull;
+  float d = __uint_as_float((unsigned)(key >> 32));
+  int idx = (int)(key & 0xffffffffu);
+  if ((double)d > .1) {
+    int t = to[idx];
+    part[idx] = t;
+    atomicAdd(&sizes[t], w[idx]);
+    atomicAdd(&sizes[p], -w[idx]);
+  }
+}
+
+// removeRuntyParts / removeRuntyPartitions (misHelpers.cu:744-820).  Returns the
+// number of removed parts.
+int remove_small_parts(Ctx& c, int n, DBuf<int32_t>& part, const int32_t* weights, int threshold_mode, int min_size,
+                       int full_size, DBuf<int32_t>& aggregated) {
+  cudaStream_t s = c.stream;
+  int np = reduce_max(part.p, n, s) + 1;
+  DBuf<int32_t> sizes(np, s), rm(np + 1, s), sub(np + 1, s);
+  sizes.zero();
+  FG_LAUNCH(histogram_kernel, grid_for(n, 256), 256, 0, s, n, part.p, weights, sizes.p);
+  int threshold = min_size;
+  if (threshold_mode == 1) {
+    double avg = (double)full_size / np;
+    threshold = (int)(avg * .7);
+  }
+  FG_LAUNCH(less_than_kernel, grid_for(np, 256), 256, 0, s, np, sizes.p, threshold, rm.p);
+  int64_t removed = exclusive_scan(rm.p, sub.p, np, s);
+  if (removed == 0 && threshold_mode == 0) return 0;
+  // subtractions = inclusive scan of the removal flags = exclusive scan shifted by one
+  FG_LAUNCH(remove_parts_kernel, grid_for(n, 256), 256, 0, s, n, part.p, rm.p, sub.p + 1, aggregated.p);
+  return (int)removed;
+}
+
+int restrict_partitions(Ctx& c, int max_size, int full_size, int n, const int32_t* xadj, const int32_t* adj,
+                        DBuf<int32_t>& part, const int32_t* w) {
+  cudaStream_t s = c.stream;
+  int np = reduce_max(part.p, n, s) + 1;
+  DBuf<int32_t> sizes(np, s), to(n, s);
+  sizes.zero();
+  FG_LAUNCH(histogram_kernel, grid_for(n, 256), 256, 0, s, n, part.p, w, sizes.p);
+  int avg = full_size / np;
+  DBuf<unsigned long long> best(np, s);
+  best.zero();
+  int largest = reduce_max(sizes.p, np, s);
+  int loops = 0;
+  while (largest > max_size) {
+    FG_REQUIRE(++loops < kCap, FEMGPU_ERR_LIMIT, "partition size restriction did not converge");
+    FG_LAUNCH(desirability_kernel, grid_for(n, 256), 256, 0, s, n, avg, xadj, adj, part.p, sizes.p, w, to.p, best.p);
+    FG_LAUNCH(swap_kernel, grid_for(np, 256), 256, 0, s, np, best.p, part.p, to.p, w, sizes.p);
+    largest = reduce_max(sizes.p, np, s);
+  }
+  return np;
+}
+
+// aggregateGraph / aggregateWeightedGraph (misHelpers.cu:513-677).
+void aggregate(Ctx& c, int n, const int32_t* xadj, const int32_t* adj, int depth, bool weighted, int min_size,
+               int max_size, int full_size, const int32_t* weights, DBuf<int32_t>& part) {
+  cudaStream_t s = c.stream;
+  DBuf<int32_t> mis;
+  random_mis(c, n, xadj, adj, depth, mis);
+  DBuf<int32_t> incl(n + 1, s), aggregated(n, s), pout(n, s), counters(2, s);
+  FG_CUDA(cudaMemcpyAsync(incl.p, mis.p, n * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
+  inclusive_scan_inplace(incl.p, n, s);
+  int mis_count = read_scalar(incl.p + (n - 1), s);
+  part.alloc(n, s);
+  FG_LAUNCH(label_roots_kernel, grid_for(n, 256), 256, 0, s, n, mis.p, incl.p, part.p, aggregated.p);
+  bool first = true;
+  for (int loop = 0;; loop++) {
+    FG_REQUIRE(loop < kCap, FEMGPU_ERR_LIMIT, "aggregation did not complete");
+    counters.zero();
+    FG_LAUNCH(allocate_kernel, grid_for(n, 256), 256, 0, s, n, xadj, adj, part.p, pout.p, aggregated.p, counters.p);
+    std::swap(part.p, pout.p);
+    int32_t h[2];
+    counters.download(h, 2);
+    FG_CUDA(cudaStreamSynchronize(s));
+    if (h[0] == 0) {
+      if (!weighted) {
+        if (remove_small_parts(c, n, part, nullptr, 0, min_size, full_size, aggregated) == 0) return;
+      } else {
+        if (!first || mis_count < 10) {
+          restrict_partitions(c, max_size, full_size, n, xadj, adj, part, weights);
+          return;
+        }
+        first = false;
+        remove_small_parts(c, n, part, weights, 1, 0, full_size, aggregated);
+      }
+      FG_REQUIRE(count_equal(aggregated.p, n, 1, s) > 0, FEMGPU_ERR_LIMIT,
+                 "every aggregate was removed as undersized (the reference loops forever here)");
+    } else if (h[1] == 0) {
+      throw Error(FEMGPU_ERR_LIMIT, "aggregation stalled: nodes unreachable from any aggregate");
+    }
+  }
+}
+
+__global__ void scatter_bucket_kernel(int n, const int32_t* key, const int32_t* start, int32_t* cursor, int32_t* out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    int k = key[i];
+    out[start[k] + atomicAdd(&cursor[k], 1)] = i;
+  }
+}
+
+__global__ void node_degree_to_agg_kernel(int n, const int32_t* xadj, const int32_t* fine, int32_t* cnt) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) atomicAdd(&cnt[fine[i]], xadj[i + 1] - xadj[i]);
+}
+
+__global__ void induced_candidates_kernel(int nagg, const int32_t* astart, const int32_t* members,
+                                          const int32_t* xadj, const int32_t* adj, const int32_t* fine,
+                                          const int32_t* coff, int32_t* cand) {
+  int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= nagg) return;
+  int o = coff[a], end = coff[a + 1];
+  for (int q = astart[a]; q < astart[a + 1]; q++) {
+    int i = members[q];
+    for (int e = xadj[i]; e < xadj[i + 1]; e++) {
+      int b = fine[adj[e]];
+      if (b != a) cand[o++] = b;
+    }
+  }
+  while (o < end) cand[o++] = INT32_MAX;  // padding, removed after the unique sort
+}
+
+__global__ void drop_padding_kernel(int nseg, const int32_t* off, int32_t* cnt, const int32_t* vals) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < nseg && cnt[k] > 0 && vals[off[k] + cnt[k] - 1] == INT32_MAX) cnt[k]--;
+}
+
+__global__ void compact_segments_kernel(int nseg, const int32_t* src, const int32_t* soff, const int32_t* doff,
+                                        int32_t* dst) {
+  int lane = threadIdx.x & 31;
+  for (int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < nseg; k += (gridDim.x * blockDim.x) >> 5) {
+    int len = doff[k + 1] - doff[k];
+    for (int t = lane; t < len; t += 32) dst[doff[k] + t] = src[soff[k] + t];
+  }
+}
+
+__global__ void invert_kernel(int n, const int32_t* order, int32_t* inv) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) inv[order[i]] = i;
+}
+
+__global__ void gather_len_kernel(int n, const int32_t* order, const int32_t* off, int32_t* len) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) len[q] = off[order[q] + 1] - off[order[q]];
+}
+
+__global__ void remap_graph_kernel(int nagg, const int32_t* old_of, const int32_t* ixadj, const int32_t* iadj,
+                                   const int32_t* new_id, const int32_t* xo, int32_t* ao) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nagg) return;
+  int a = old_of[q];
+  int o = xo[q];
+  for (int e = ixadj[a]; e < ixadj[a + 1]; e++) ao[o++] = new_id[iadj[e]];
+}
+
+__global__ void node_order_kernel(int nagg, const int32_t* old_of, const int32_t* astart, const int32_t* members,
+                                  const int32_t* agg_idx, const int32_t* coarse, int32_t* iperm, int32_t* agg_of,
+                                  int32_t* part_of_row) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nagg) return;
+  int a = old_of[q];
+  int o = agg_idx[q];
+  int p = coarse[a];
+  for (int t = astart[a]; t < astart[a + 1]; t++) {
+    iperm[o] = members[t];
+    agg_of[o] = q;
+    part_of_row[o] = p;
+    o++;
+  }
+}
+
+struct OldMisOut {
+  int nagg = 0, npart = 0;
+  DBuf<int32_t> perm, iperm, agg_idx, part_idx, agg_of, part_of_row, xadj_out, adj_out;
+  int64_t nnz_out = 0;
+};
+
+// misHelpers::CP::OldMIS (ComputePermutationMethods.cu:22-151).
+void old_mis(Ctx& c, int n, const int32_t* xadj, const int32_t* adj, OldMisOut& o) {
+  cudaStream_t s = c.stream;
+  const int params = c.cfg.randMisParameters;
+  const int fine_depth = params % 100, coarse_depth = (params / 100) % 100, min_agg = (params / 10000) % 10;
+  DBuf<int32_t> fine;
+  aggregate(c, n, xadj, adj, fine_depth, false, min_agg, 0, n, nullptr, fine);
+  const int nagg = reduce_max(fine.p, n, s) + 1;
+  // aggregate member lists, ascending node id
+  DBuf<int32_t> acount(nagg + 1, s), astart(nagg + 1, s), cursor(nagg, s), members(n, s);
+  acount.zero();
+  FG_LAUNCH(histogram_kernel, grid_for(n, 256), 256, 0, s, n, fine.p, nullptr, acount.p);
+  exclusive_scan(acount.p, astart.p, nagg, s);
+  cursor.zero();
+  FG_LAUNCH(scatter_bucket_kernel, grid_for(n, 256), 256, 0, s, n, fine.p, astart.p, cursor.p, members.p);
+  segmented_sort_i32(members.p, astart.p, nagg, nullptr, s);
+  // induced graph (getInducedGraph, misHelpers.cu:1078-1107): sorted unique neighbour aggregates
+  DBuf<int32_t> ccount(nagg + 1, s), coff(nagg + 1, s);
+  ccount.zero();
+  FG_LAUNCH(node_degree_to_agg_kernel, grid_for(n, 256), 256, 0, s, n, xadj, fine.p, ccount.p);
+  int64_t ncand = exclusive_scan(ccount.p, coff.p, nagg, s);
+  DBuf<int32_t> cand(ncand > 0 ? ncand : 1, s), ucount(nagg + 1, s), ixadj(nagg + 1, s);
+  FG_LAUNCH(induced_candidates_kernel, grid_for(nagg, 128), 128, 0, s, nagg, astart.p, members.p, xadj, adj, fine.p,
+            coff.p, cand.p);
+  segmented_sort_i32(cand.p, coff.p, nagg, ucount.p, s);
+  FG_LAUNCH(drop_padding_kernel, grid_for(nagg, 256), 256, 0, s, nagg, coff.p, ucount.p, cand.p);
+  int64_t innz = exclusive_scan(ucount.p, ixadj.p, nagg, s);
+  DBuf<int32_t> iadj(innz > 0 ? innz : 1, s);
+  FG_LAUNCH(compact_segments_kernel, grid_for((int64_t)nagg * 32, 256), 256, 0, s, nagg, cand.p, coff.p, ixadj.p,
+            iadj.p);
+  // partitions of aggregates (aggregateWeightedGraph, weights = aggregate sizes)
+  DBuf<int32_t> coarse;
+  aggregate(c, nagg, ixadj.p, iadj.p, coarse_depth, true, 0, c.cfg.partitionMaxSize, n, acount.p, coarse);
+  const int npart = reduce_max(coarse.p, nagg, s) + 1;
+  // new aggregate ids: order (partition, old id)
+  DBuf<int32_t> pcount(npart + 1, s), pcur(npart, s), old_of(nagg, s), new_id(nagg, s);
+  pcount.zero();
+  FG_LAUNCH(histogram_kernel, grid_for(nagg, 256), 256, 0, s, nagg, coarse.p, nullptr, pcount.p);
+  o.part_idx.alloc(npart + 1, s);
+  exclusive_scan(pcount.p, o.part_idx.p, npart, s);
+  pcur.zero();
+  FG_LAUNCH(scatter_bucket_kernel, grid_for(nagg, 256), 256, 0, s, nagg, coarse.p, o.part_idx.p, pcur.p, old_of.p);
+  segmented_sort_i32(old_of.p, o.part_idx.p, npart, nullptr, s);
+  FG_LAUNCH(invert_kernel, grid_for(nagg, 256), 256, 0, s, nagg, old_of.p, new_id.p);
+  // next-level graph (remapInducedGraph, misHelpers.cu:1258-1280): rows in new order,
+  // entries kept in their order and renamed
+  DBuf<int32_t> rlen(nagg + 1, s);
+  FG_LAUNCH(gather_len_kernel, grid_for(nagg, 256), 256, 0, s, nagg, old_of.p, ixadj.p, rlen.p);
+  o.xadj_out.alloc(nagg + 1, s);
+  o.nnz_out = exclusive_scan(rlen.p, o.xadj_out.p, nagg, s);
+  o.adj_out.alloc(o.nnz_out > 0 ? o.nnz_out : 1, s);
+  FG_LAUNCH(remap_graph_kernel, grid_for(nagg, 256), 256, 0, s, nagg, old_of.p, ixadj.p, iadj.p, new_id.p,
+            o.xadj_out.p, o.adj_out.p);
+  // node order: aggregates in new order, members ascending
+  DBuf<int32_t> asz(nagg + 1, s);
+  FG_LAUNCH(gather_len_kernel, grid_for(nagg, 256), 256, 0, s, nagg, old_of.p, astart.p, asz.p);
+  o.agg_idx.alloc(nagg + 1, s);
+  exclusive_scan(asz.p, o.agg_idx.p, nagg, s);
+  o.iperm.alloc(n, s);
+  o.perm.alloc(n, s);
+  o.agg_of.alloc(n, s);
+  o.part_of_row.alloc(n, s);
+  FG_LAUNCH(node_order_kernel, grid_for(nagg, 256), 256, 0, s, nagg, old_of.p, astart.p, members.p, o.agg_idx.p,
+            coarse.p, o.iperm.p, o.agg_of.p, o.part_of_row.p);
+  FG_LAUNCH(invert_kernel, grid_for(n, 256), 256, 0, s, n, o.iperm.p, o.perm.p);
+  o.nagg = nagg;
+  o.npart = npart;
+}
+
+// ---------------------------------------------------------------------------------
+// Row-wise expand-sort-compress in shared memory.
+//
+// Each output row is generated as a list of (column, value) items in a fixed
+// generation order, sorted stably by column, and every run of equal columns is
+// summed left to right from its first item.  Modes:
+//   PERMUTE  row i <- input row iperm[i], columns renamed by perm (no duplicates);
+//   PROLONG  row i of Ap: items (agg_of[j], ((-omega) a_ij) / d_i), then (agg_of[i], 1)
+//            (generateProlongatorFull_d, smoothedMG_amg_level.cu:321-387);
+//   SPGEMM   row i of A*B: items (k, a_ij b_jk) for j ascending, then k ascending
+//            (the product of generateNextLevelMatrixFull_d, :390-400).
+// Pass 0 writes per-row item counts, pass 1 unique counts, pass 2 the row.
+enum EscMode { ESC_PERMUTE = 0, ESC_PROLONG = 1, ESC_SPGEMM = 2 };
+
+template <class T>
+struct EscArgs {
+  int n;
+  const int32_t* arp;
+  const int32_t* aci;
+  const T* av;
+  const int32_t* brp;
+  const int32_t* bci;
+  const T* bv;
+  const int32_t* perm;   // PERMUTE: old->new column map (nullptr = identity)
+  const int32_t* iperm;  // PERMUTE: output row -> input row (nullptr = identity)
+  const int32_t* agg_of; // PROLONG
+  const T* diag;         // PROLONG
+  T neg_omega;           // PROLONG
+  const int32_t* big_rows;  // block tier: list of rows
+  int nbig;
+  int32_t* counts;       // pass 0/1 output
+  const int32_t* orp;    // pass 2: output row offsets
+  int32_t* oci;
+  T* ov;
+  int32_t* overflow;
+};
+
+constexpr int kEscWarpCap = 512;
+constexpr int kEscWarps = 4;
+constexpr int kEscBlockCap = 8192;
+constexpr int kEscBlockThreads = 512;
+
+template <class T, int MODE>
+__device__ __forceinline__ int esc_input_row(const EscArgs<T>& a, int i) {
+  return (MODE == ESC_PERMUTE && a.iperm) ? a.iperm[i] : i;
+}
+
+// Number of items of row i.
+template <class T, int MODE>
+__device__ __forceinline__ int esc_row_items(const EscArgs<T>& a, int i) {
+  int r = esc_input_row<T, MODE>(a, i);
+  int b = a.arp[r], e = a.arp[r + 1];
+  if (MODE == ESC_PERMUTE) return e - b;
+  if (MODE == ESC_PROLONG) return e - b + 1;
+  int s = 0;
+  for (int q = b; q < e; q++) {
+    int j = a.aci[q];
+    s += a.brp[j + 1] - a.brp[j];
+  }
+  return s;
+}
+
+// Generates row i's items into keys (column << 32 | generation index) and vals.
+// tid/nthr: cooperating threads; sync: their barrier.
+template <class T, int MODE, class Sync>
+__device__ void esc_generate(const EscArgs<T>& a, int i, unsigned long long* keys, T* vals, int tid, int nthr,
+                             int* s_scan, Sync sync) {
+  int r = esc_input_row<T, MODE>(a, i);
+  int b = a.arp[r], e = a.arp[r + 1];
+  if (MODE != ESC_SPGEMM) {
+    for (int q = b + tid; q < e; q += nthr) {
+      int g = q - b;
+      int j = a.aci[q];
+      int col;
+      T v;
+      if (MODE == ESC_PERMUTE) {
+        col = a.perm ? a.perm[j] : j;
+        v = a.av[q];
+      } else {
+        col = a.agg_of[j];
+        T t = (a.neg_omega * a.av[q]) * (T)1;
+        v = t / a.diag[i];
+      }
+      keys[g] = ((unsigned long long)(unsigned)col << 32) | (unsigned)g;
+      vals[g] = v;
+    }
+    if (MODE == ESC_PROLONG && tid == 0) {
+      int g = e - b;
+      keys[g] = ((unsigned long long)(unsigned)a.agg_of[i] << 32) | (unsigned)g;
+      vals[g] = (T)1;
+    }
+    return;
+  }
+  // SPGEMM: chunks of nthr A entries; offsets by an exclusive scan of B row lengths
+  int base = 0;
+  for (int c0 = b; c0 < e; c0 += nthr) {
+    int q = c0 + tid;
+    int len = 0, j = 0;
+    if (q < e) {
+      j = a.aci[q];
+      len = a.brp[j + 1] - a.brp[j];
+    }
+    // block/warp exclusive scan of len via shared memory (nthr <= 512)
+    s_scan[tid] = len;
+    sync();
+    for (int off = 1; off < nthr; off <<= 1) {
+      int add = tid >= off ? s_scan[tid - off] : 0;
+      sync();
+      s_scan[tid] += add;
+      sync();
+    }
+    int excl = s_scan[tid] - len;
+    int total = s_scan[nthr - 1];
+    sync();
+    if (q < e) {
+      T av = a.av[q];
+      int jb = a.brp[j];
+      for (int t = 0; t < len; t++) {
+        int g = base + excl + t;
+        keys[g] = ((unsigned long long)(unsigned)a.bci[jb + t] << 32) | (unsigned)g;
+        vals[g] = av * a.bv[jb + t];
+      }
+    }
+    base += total;
+  }
+}
+
+// After sorting: count (pass 1) or write (pass 2) the reduced row.
+template <class T, class Sync>
+__device__ int esc_reduce(const unsigned long long* keys, const T* vals_by_gen, int len, int tid, int nthr, int* s_cnt,
+                          int32_t* oci, T* ov, bool write, Sync sync) {
+  // heads: positions whose column differs from the previous one
+  if (tid == 0) *s_cnt = 0;
+  sync();
+  // count heads per thread-chunk sequentially in a fixed chunk order
+  int total = 0;
+  for (int c0 = 0; c0 < len; c0 += nthr) {
+    int p = c0 + tid;
+    bool head = p < len && (p == 0 || (keys[p] >> 32) != (keys[p - 1] >> 32));
+    // rank among heads within this chunk
+    __shared__ int s_flags[kEscBlockThreads];
+    int* flags = s_flags + ((nthr == 32) ? (threadIdx.x & ~31) : 0);
+    flags[tid] = head ? 1 : 0;
+    sync();
+    int rank = 0, chunk_heads = 0;
+    if (nthr == 32) {
+      unsigned m = __ballot_sync(0xffffffffu, head);
+      rank = __popc(m & ((1u << tid) - 1u));
+      chunk_heads = __popc(m);
+    } else {
+      for (int t = 0; t < nthr; t++) {
+        if (t < tid) rank += flags[t];
+        chunk_heads += flags[t];
+      }
+    }
+    if (head && write) {
+      unsigned col = (unsigned)(keys[p] >> 32);
+      T sum = vals_by_gen[(unsigned)(keys[p] & 0xffffffffu)];
+      for (int q = p + 1; q < len && (unsigned)(keys[q] >> 32) == col; q++)
+        sum = sum + vals_by_gen[(unsigned)(keys[q] & 0xffffffffu)];
+      oci[total + rank] = (int32_t)col;
+      ov[total + rank] = sum;
+    }
+    total += chunk_heads;
+    sync();
+  }
+  return total;
+}
+
+template <class T, int MODE>
+__global__ void esc_count_items_kernel(EscArgs<T> a) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < a.n) a.counts[i] = esc_row_items<T, MODE>(a, i);
+}
+
+__global__ void collect_big_rows_kernel(int n, const int32_t* items, int cap, int32_t* list, int32_t* nlist,
+                                        int32_t* overflow, int hard_cap) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && items[i] > cap) {
+    if (items[i] > hard_cap) atomicExch(overflow, 1);
+    else list[atomicAdd(nlist, 1)] = i;
+  }
+}
+
+template <class T, int MODE, bool WRITE>
+__global__ void esc_warp_kernel(EscArgs<T> a, const int32_t* items) {
+  extern __shared__ unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  unsigned long long* keys = reinterpret_cast<unsigned long long*>(smem_raw) + (size_t)w * kEscWarpCap;
+  T* vals = reinterpret_cast<T*>(reinterpret_cast<unsigned long long*>(smem_raw) + (size_t)kEscWarps * kEscWarpCap) +
+            (size_t)w * kEscWarpCap;
+  __shared__ int s_scan[kEscWarps][32];
+  __shared__ int s_cnt[kEscWarps];
+  for (int i = blockIdx.x * kEscWarps + w; i < a.n; i += gridDim.x * kEscWarps) {
+    int len = items[i];
+    if (len > kEscWarpCap) continue;
+    esc_generate<T, MODE>(a, i, keys, vals, lane, 32, s_scan[w], WarpSync());
+    int np2 = next_pow2(len < 2 ? 2 : len);
+    for (int p = len + lane; p < np2; p += 32) keys[p] = ~0ull;
+    __syncwarp();
+    bitonic_sort_shared(keys, np2, lane, 32, WarpSync());
+    int out = WRITE ? a.orp[i] : 0;
+    int cnt = esc_reduce<T>(keys, vals, len, lane, 32, &s_cnt[w], WRITE ? a.oci + out : nullptr,
+                            WRITE ? a.ov + out : nullptr, WRITE, WarpSync());
+    if (!WRITE && lane == 0) a.counts[i] = cnt;
+    __syncwarp();
+  }
+}
+
+template <class T, int MODE, bool WRITE>
+__global__ void esc_block_kernel(EscArgs<T> a, const int32_t* items) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned long long* keys = reinterpret_cast<unsigned long long*>(smem_raw);
+  T* vals = reinterpret_cast<T*>(keys + kEscBlockCap);
+  __shared__ int s_scan[kEscBlockThreads];
+  __shared__ int s_cnt;
+  for (int b = blockIdx.x; b < a.nbig; b += gridDim.x) {
+    int i = a.big_rows[b];
+    int len = items[i];
+    esc_generate<T, MODE>(a, i, keys, vals, threadIdx.x, blockDim.x, s_scan, BlockSync());
+    int np2 = next_pow2(len);
+    for (int p = len + threadIdx.x; p < np2; p += blockDim.x) keys[p] = ~0ull;
+    __syncthreads();
+    bitonic_sort_shared(keys, np2, threadIdx.x, blockDim.x, BlockSync());
+    int out = WRITE ? a.orp[i] : 0;
+    int cnt = esc_reduce<T>(keys, vals, len, threadIdx.x, blockDim.x, &s_cnt, WRITE ? a.oci + out : nullptr,
+                            WRITE ? a.ov + out : nullptr, WRITE, BlockSync());
+    if (!WRITE && threadIdx.x == 0) a.counts[i] = cnt;
+    __syncthreads();
+  }
+}
+
+template <class T, int MODE>
+void run_esc(Ctx& c, EscArgs<T> a, int nrows_out, int ncols_out, DCsr<T>& out) {
+  cudaStream_t s = c.stream;
+  a.n = nrows_out;
+  DBuf<int32_t> items(nrows_out + 1, s), ucnt(nrows_out + 1, s), big(nrows_out + 1, s), nbig(1, s), ovf(1, s);
+  nbig.zero();
+  ovf.zero();
+  a.counts = items.p;
+  FG_LAUNCH((esc_count_items_kernel<T, MODE>), grid_for(nrows_out, 256), 256, 0, s, a);
+  FG_LAUNCH(collect_big_rows_kernel, grid_for(nrows_out, 256), 256, 0, s, nrows_out, items.p, kEscWarpCap, big.p,
+            nbig.p, ovf.p, kEscBlockCap);
+  FG_REQUIRE(read_scalar(ovf.p, s) == 0, FEMGPU_ERR_LIMIT,
+             "a sparse row has more than 8192 products (row-wise SpGEMM capacity)");
+  a.nbig = read_scalar(nbig.p, s);
+  a.big_rows = big.p;
+  const size_t wsm = (size_t)kEscWarps * kEscWarpCap * (sizeof(unsigned long long) + sizeof(T));
+  const size_t bsm = (size_t)kEscBlockCap * (sizeof(unsigned long long) + sizeof(T));
+  static bool attr_set = false;
+  if (!attr_set) {
+    FG_CUDA(cudaFuncSetAttribute(esc_warp_kernel<T, MODE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
+    FG_CUDA(cudaFuncSetAttribute(esc_warp_kernel<T, MODE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
+    FG_CUDA(cudaFuncSetAttribute(esc_block_kernel<T, MODE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsm));
+    FG_CUDA(cudaFuncSetAttribute(esc_block_kernel<T, MODE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsm));
+    attr_set = true;
+  }
+  const int wgrid = std::min<int64_t>((nrows_out + kEscWarps - 1) / kEscWarps, 152 * 64);
+  a.counts = ucnt.p;
+  FG_LAUNCH((esc_warp_kernel<T, MODE, false>), wgrid, 32 * kEscWarps, wsm, s, a, items.p);
+  if (a.nbig > 0)
+    FG_LAUNCH((esc_block_kernel<T, MODE, false>), std::min(a.nbig, 152 * 2), kEscBlockThreads, bsm, s, a, items.p);
+  out.n = nrows_out;
+  out.m = ncols_out;
+  out.rp.alloc(nrows_out + 1, s);
+  out.nnz = exclusive_scan(ucnt.p, out.rp.p, nrows_out, s);
+  out.ci.alloc(out.nnz > 0 ? out.nnz : 1, s);
+  out.v.alloc(out.nnz > 0 ? out.nnz : 1, s);
+  a.orp = out.rp.p;
+  a.oci = out.ci.p;
+  a.ov = out.v.p;
+  FG_LAUNCH((esc_warp_kernel<T, MODE, true>), wgrid, 32 * kEscWarps, wsm, s, a, items.p);
+  if (a.nbig > 0)
+    FG_LAUNCH((esc_block_kernel<T, MODE, true>), std::min(a.nbig, 152 * 2), kEscBlockThreads, bsm, s, a, items.p);
+}
+
+// ---- level matrices -----------------------------------------------------------------
+template <class T>
+__global__ void diag_kernel(int n, const int32_t* rp, const int32_t* ci, const T* v, T* d) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    int s = lower_bound_i32(ci, rp[i], rp[i + 1], i);
+    d[i] = (s < rp[i + 1] && ci[s] == i) ? v[s] : (T)0;
+  }
+}
+
+template <class T>
+__global__ void split_count_kernel(int n, const int32_t* rp, const int32_t* ci, const int32_t* part, int32_t* cin,
+                                   int32_t* cout) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int pi = part[i], a = 0, b = 0;
+  for (int e = rp[i]; e < rp[i + 1]; e++) {
+    int j = ci[e];
+    if (j == i) continue;
+    if (part[j] == pi) a++;
+    else b++;
+  }
+  cin[i] = a;
+  cout[i] = b;
+}
+
+template <class T>
+__global__ void split_fill_kernel(int n, const int32_t* rp, const int32_t* ci, const T* v, const int32_t* part,
+                                  const int32_t* irp, int32_t* ici, T* iv, const int32_t* orp, int32_t* oci, T* ov) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int pi = part[i], qi = irp[i], qo = orp[i];
+  for (int e = rp[i]; e < rp[i + 1]; e++) {
+    int j = ci[e];
+    if (j == i) continue;
+    if (part[j] == pi) {
+      T val = v[e];
+      if (j < i) {  // the symmetric smoother reads the upper entry (j, i) for both
+        int u = lower_bound_i32(ci, rp[j], rp[j + 1], i);
+        val = (u < rp[j + 1] && ci[u] == i) ? v[u] : (T)0;
+      }
+      ici[qi] = j;
+      iv[qi] = val;
+      qi++;
+    } else {
+      oci[qo] = j;
+      ov[qo] = v[e];
+      qo++;
+    }
+  }
+}
+
+template <class T>
+__global__ void transpose_count_kernel(int64_t nnz, const int32_t* ci, int32_t* cnt) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nnz; e += (int64_t)gridDim.x * blockDim.x)
+    atomicAdd(&cnt[ci[e]], 1);
+}
+
+template <class T>
+__global__ void transpose_fill_kernel(int n, const int32_t* rp, const int32_t* ci, const T* v, const int32_t* trp,
+                                      int32_t* cur, int32_t* tci, T* tv) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int e = rp[i]; e < rp[i + 1]; e++) {
+    int k = ci[e];
+    int q = trp[k] + atomicAdd(&cur[k], 1);
+    tci[q] = i;
+    tv[q] = v[e];
+  }
+}
+
+template <class T>
+__global__ void cast_kernel(int64_t n, const double* in, T* out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (T)in[i];
+}
+
+template <class T>
+__global__ void densify_kernel(int n, const int32_t* rp, const int32_t* ci, const T* v, double* F) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n)
+    for (int e = rp[i]; e < rp[i + 1]; e++) F[(int64_t)i * n + ci[e]] = (double)v[e];
+}
+
+// Dense LU with partial pivoting (first maximal |pivot| in row order), one block.
+__global__ void dense_lu_kernel(int n, double* F, int32_t* piv, int32_t* status) {
+  __shared__ double s_best[1024];
+  __shared__ int s_idx[1024];
+  for (int k = 0; k < n; k++) {
+    double best = -1.0;
+    int bi = n;
+    for (int i = k + threadIdx.x; i < n; i += blockDim.x) {
+      double a = fabs(F[(int64_t)i * n + k]);
+      if (a > best || (a == best && i < bi)) {
+        best = a;
+        bi = i;
+      }
+    }
+    s_best[threadIdx.x] = best;
+    s_idx[threadIdx.x] = bi;
+    __syncthreads();
+    for (int off = blockDim.x >> 1; off > 0; off >>= 1) {
+      if (threadIdx.x < off) {
+        double ob = s_best[threadIdx.x + off];
+        int oi = s_idx[threadIdx.x + off];
+        if (ob > s_best[threadIdx.x] || (ob == s_best[threadIdx.x] && oi < s_idx[threadIdx.x])) {
+          s_best[threadIdx.x] = ob;
+          s_idx[threadIdx.x] = oi;
+        }
+      }
+      __syncthreads();
+    }
+    int p = s_idx[0];
+    double pb = s_best[0];
+    __syncthreads();
+    if (pb == 0.0) {
+      if (threadIdx.x == 0) *status = 1;
+      return;
+    }
+    if (threadIdx.x == 0) piv[k] = p;
+    if (p != k)
+      for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        double t = F[(int64_t)k * n + j];
+        F[(int64_t)k * n + j] = F[(int64_t)p * n + j];
+        F[(int64_t)p * n + j] = t;
+      }
+    __syncthreads();
+    double d = F[(int64_t)k * n + k];
+    for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) F[(int64_t)i * n + k] = F[(int64_t)i * n + k] / d;
+    __syncthreads();
+    for (int64_t q = threadIdx.x; q < (int64_t)(n - k - 1) * (n - k - 1); q += blockDim.x) {
+      int i = k + 1 + (int)(q / (n - k - 1));
+      int j = k + 1 + (int)(q % (n - k - 1));
+      F[(int64_t)i * n + j] = fma(-F[(int64_t)i * n + k], F[(int64_t)k * n + j], F[(int64_t)i * n + j]);
+    }
+    __syncthreads();
+  }
+}
+
+// Column j of the inverse: solve LU x = P e_j with the factor (one thread per column).
+__global__ void dense_inverse_kernel(int n, const double* F, const int32_t* piv, double* work, double* inv) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  double* b = work + (int64_t)j * n;
+  for (int i = 0; i < n; i++) b[i] = (i == j) ? 1.0 : 0.0;
+  for (int k = 0; k < n; k++) {
+    double t = b[k];
+    b[k] = b[piv[k]];
+    b[piv[k]] = t;
+  }
+  for (int i = 0; i < n; i++) {
+    double s = b[i];
+    for (int q = 0; q < i; q++) s = fma(-F[(int64_t)i * n + q], b[q], s);
+    b[i] = s;
+  }
+  for (int i = n - 1; i >= 0; i--) {
+    double s = b[i];
+    for (int q = i + 1; q < n; q++) s = fma(-F[(int64_t)i * n + q], b[q], s);
+    b[i] = s / F[(int64_t)i * n + i];
+  }
+  for (int i = 0; i < n; i++) inv[(int64_t)i * n + j] = b[i];
+}
+
+__global__ void partition_rows_kernel(int npart, const int32_t* part_idx, const int32_t* agg_idx, int32_t* rows) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < npart) rows[p] = agg_idx[part_idx[p + 1]] - agg_idx[part_idx[p]];
+}
+
+template <class T>
+void build_levels(Ctx& c, Hierarchy<T>& H) {
+  cudaStream_t s = c.stream;
+  const int n0 = c.A.n;
+  // level 0: the operator converted to T
+  {
+    auto L0 = std::make_unique<Level<T>>();
+    L0->n = n0;
+    L0->A.n = L0->A.m = n0;
+    L0->A.nnz = c.A.nnz;
+    L0->A.rp.alloc(n0 + 1, s);
+    L0->A.ci.alloc(c.A.nnz, s);
+    L0->A.v.alloc(c.A.nnz, s);
+    FG_CUDA(cudaMemcpyAsync(L0->A.rp.p, c.A.rp.p, (n0 + 1) * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
+    FG_CUDA(cudaMemcpyAsync(L0->A.ci.p, c.A.ci.p, c.A.nnz * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
+    FG_LAUNCH(cast_kernel<T>, grid_for(c.A.nnz, 256), 256, 0, s, c.A.nnz, c.A.v.p, L0->A.v.p);
+    L0->gnnz = c.graph_nnz;
+    L0->gxadj.alloc(n0 + 1, s);
+    L0->gadj.alloc(c.graph_nnz > 0 ? c.graph_nnz : 1, s);
+    FG_CUDA(cudaMemcpyAsync(L0->gxadj.p, c.gxadj.p, (n0 + 1) * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
+    if (c.graph_nnz > 0)
+      FG_CUDA(cudaMemcpyAsync(L0->gadj.p, c.gadj.p, c.graph_nnz * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
+    H.L.push_back(std::move(L0));
+  }
+  int num_levels = 1;
+  while (true) {
+    Level<T>& L = *H.L.back();
+    const int N = L.A.n;
+    if (N < c.cfg.topSize || num_levels >= c.cfg.maxLevels) {
+      FG_REQUIRE(N <= 8192, FEMGPU_ERR_LIMIT, "coarsest level too large for the dense solve (raise maxLevels)");
+      L.coarsest = true;
+      DBuf<double> F((size_t)N * N, s), work((size_t)N * N, s);
+      DBuf<int32_t> piv(N, s), st(1, s);
+      F.zero();
+      st.zero();
+      FG_LAUNCH(densify_kernel<T>, grid_for(N, 128), 128, 0, s, N, L.A.rp.p, L.A.ci.p, L.A.v.p, F.p);
+      FG_LAUNCH(dense_lu_kernel, 1, 1024, 0, s, N, F.p, piv.p, st.p);
+      FG_REQUIRE(read_scalar(st.p, s) == 0, FEMGPU_ERR_BREAKDOWN, "coarsest matrix is singular");
+      L.Ainv.alloc((size_t)N * N, s);
+      FG_LAUNCH(dense_inverse_kernel, grid_for(N, 64), 64, 0, s, N, F.p, piv.p, work.p, L.Ainv.p);
+      L.b.alloc(N, s);
+      L.x.alloc(N, s);
+      break;
+    }
+    OldMisOut o;
+    old_mis(c, N, L.gxadj.p, L.gadj.p, o);
+    L.nagg = o.nagg;
+    L.npart = o.npart;
+    L.perm = std::move(o.perm);
+    L.iperm = std::move(o.iperm);
+    L.agg_idx = std::move(o.agg_idx);
+    L.part_idx = std::move(o.part_idx);
+    L.agg_of = std::move(o.agg_of);
+    // permuted operator
+    {
+      EscArgs<T> a{};
+      a.arp = L.A.rp.p;
+      a.aci = L.A.ci.p;
+      a.av = L.A.v.p;
+      a.perm = L.perm.p;
+      a.iperm = L.iperm.p;
+      run_esc<T, ESC_PERMUTE>(c, a, N, N, L.Ap);
+    }
+    L.diag.alloc(N, s);
+    FG_LAUNCH(diag_kernel<T>, grid_for(N, 256), 256, 0, s, N, L.Ap.rp.p, L.Ap.ci.p, L.Ap.v.p, L.diag.p);
+    // in/out-of-partition split
+    {
+      DBuf<int32_t> cin(N + 1, s), cout(N + 1, s);
+      FG_LAUNCH(split_count_kernel<T>, grid_for(N, 256), 256, 0, s, N, L.Ap.rp.p, L.Ap.ci.p, o.part_of_row.p, cin.p,
+                cout.p);
+      L.Ain.n = L.Ain.m = L.Aout.n = L.Aout.m = N;
+      L.Ain.rp.alloc(N + 1, s);
+      L.Aout.rp.alloc(N + 1, s);
+      L.Ain.nnz = exclusive_scan(cin.p, L.Ain.rp.p, N, s);
+      L.Aout.nnz = exclusive_scan(cout.p, L.Aout.rp.p, N, s);
+      L.Ain.ci.alloc(L.Ain.nnz > 0 ? L.Ain.nnz : 1, s);
+      L.Ain.v.alloc(L.Ain.nnz > 0 ? L.Ain.nnz : 1, s);
+      L.Aout.ci.alloc(L.Aout.nnz > 0 ? L.Aout.nnz : 1, s);
+      L.Aout.v.alloc(L.Aout.nnz > 0 ? L.Aout.nnz : 1, s);
+      FG_LAUNCH(split_fill_kernel<T>, grid_for(N, 256), 256, 0, s, N, L.Ap.rp.p, L.Ap.ci.p, L.Ap.v.p,
+                o.part_of_row.p, L.Ain.rp.p, L.Ain.ci.p, L.Ain.v.p, L.Aout.rp.p, L.Aout.ci.p, L.Aout.v.p);
+    }
+    {
+      DBuf<int32_t> prow(L.npart + 1, s);
+      FG_LAUNCH(partition_rows_kernel, grid_for(L.npart, 256), 256, 0, s, L.npart, L.part_idx.p, L.agg_idx.p, prow.p);
+      L.max_part_rows = reduce_max(prow.p, L.npart, s);
+    }
+    // prolongator and restrictor
+    {
+      EscArgs<T> a{};
+      a.arp = L.Ap.rp.p;
+      a.aci = L.Ap.ci.p;
+      a.av = L.Ap.v.p;
+      a.agg_of = L.agg_of.p;
+      a.diag = L.diag.p;
+      a.neg_omega = -(T)c.cfg.proOmega;
+      run_esc<T, ESC_PROLONG>(c, a, N, L.nagg, L.P);
+    }
+    {
+      DCsr<T> Ru;  // unsorted transpose, then rows sorted by column
+      Ru.n = L.nagg;
+      Ru.m = N;
+      Ru.nnz = L.P.nnz;
+      DBuf<int32_t> cnt(L.nagg + 1, s), cur(L.nagg, s);
+      cnt.zero();
+      cur.zero();
+      FG_LAUNCH(transpose_count_kernel<T>, grid_for(L.P.nnz, 256), 256, 0, s, L.P.nnz, L.P.ci.p, cnt.p);
+      Ru.rp.alloc(L.nagg + 1, s);
+      exclusive_scan(cnt.p, Ru.rp.p, L.nagg, s);
+      Ru.ci.alloc(L.P.nnz, s);
+      Ru.v.alloc(L.P.nnz, s);
+      FG_LAUNCH(transpose_fill_kernel<T>, grid_for(N, 256), 256, 0, s, N, L.P.rp.p, L.P.ci.p, L.P.v.p, Ru.rp.p, cur.p,
+                Ru.ci.p, Ru.v.p);
+      EscArgs<T> a{};
+      a.arp = Ru.rp.p;
+      a.aci = Ru.ci.p;
+      a.av = Ru.v.p;
+      run_esc<T, ESC_PERMUTE>(c, a, L.nagg, N, L.R);
+    }
+    // Galerkin product A_next = R (Ap P)
+    auto nx = std::make_unique<Level<T>>();
+    {
+      DCsr<T> AP;
+      EscArgs<T> a{};
+      a.arp = L.Ap.rp.p;
+      a.aci = L.Ap.ci.p;
+      a.av = L.Ap.v.p;
+      a.brp = L.P.rp.p;
+      a.bci = L.P.ci.p;
+      a.bv = L.P.v.p;
+      run_esc<T, ESC_SPGEMM>(c, a, N, L.nagg, AP);
+      EscArgs<T> r{};
+      r.arp = L.R.rp.p;
+      r.aci = L.R.ci.p;
+      r.av = L.R.v.p;
+      r.brp = AP.rp.p;
+      r.bci = AP.ci.p;
+      r.bv = AP.v.p;
+      run_esc<T, ESC_SPGEMM>(c, r, L.nagg, L.nagg, nx->A);
+    }
+    nx->n = L.nagg;
+    nx->gxadj = std::move(o.xadj_out);
+    nx->gadj = std::move(o.adj_out);
+    nx->gnnz = o.nnz_out;
+    // work vectors
+    L.b.alloc(N, s);
+    L.x.alloc(N, s);
+    L.r.alloc(N, s);
+    L.xo.alloc(N, s);
+    L.t.alloc(N, s);
+    H.L.push_back(std::move(nx));
+    num_levels++;
+  }
+  H.num_levels = num_levels;
+}
+
+__global__ void identity_kernel(int n, int32_t* p) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = i;
+}
+
+}  // namespace
+
+std::atomic<int64_t> g_kernel_launches{0};
+
+void amg_setup(Ctx& c) {
+  cudaStream_t s = c.stream;
+  FG_REQUIRE(c.has_matrix, FEMGPU_ERR_NOT_READY, "no operator: call femgpu_set_mesh + femgpu_assemble or femgpu_set_matrix_csr");
+  FG_REQUIRE(c.cfg.aggregatorType == 0, FEMGPU_ERR_INVALID, "only aggregatorType 0 (OldMIS) is implemented");
+  cudaEvent_t e0, e1;
+  FG_CUDA(cudaEventCreate(&e0));
+  FG_CUDA(cudaEventCreate(&e1));
+  FG_CUDA(cudaEventRecord(e0, s));
+  c.H.reset();
+  c.has_hierarchy = false;
+  const int n = c.A.n;
+  const int32_t* perm0 = nullptr;
+  if (c.cfg.precision == 1) {
+    auto H = std::make_unique<Hierarchy<double>>();
+    build_levels(c, *H);
+    if (!H->L[0]->coarsest) perm0 = H->L[0]->perm.p;
+    c.H = std::move(H);
+  } else {
+    auto H = std::make_unique<Hierarchy<float>>();
+    build_levels(c, *H);
+    if (!H->L[0]->coarsest) perm0 = H->L[0]->perm.p;
+    c.H = std::move(H);
+  }
+  c.perm0.alloc(n, s);
+  if (perm0)
+    FG_CUDA(cudaMemcpyAsync(c.perm0.p, perm0, n * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
+  else
+    FG_LAUNCH(identity_kernel, grid_for(n, 256), 256, 0, s, n, c.perm0.p);
+  // FP64 outer operator in level-0 order
+  {
+    DBuf<int32_t> iperm(n, s);
+    FG_LAUNCH(invert_kernel, grid_for(n, 256), 256, 0, s, n, c.perm0.p, iperm.p);
+    EscArgs<double> a{};
+    a.arp = c.A.rp.p;
+    a.aci = c.A.ci.p;
+    a.av = c.A.v.p;
+    a.perm = c.perm0.p;
+    a.iperm = iperm.p;
+    run_esc<double, ESC_PERMUTE>(c, a, n, n, c.A0p);
+  }
+  FG_CUDA(cudaEventRecord(e1, s));
+  FG_CUDA(cudaEventSynchronize(e1));
+  float ms = 0;
+  FG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  c.setup_ms = ms;
+  c.has_hierarchy = true;
+}
+
+}  // namespace femgpu

@@ -1,0 +1,505 @@
+// amg_solve.cu -- V-cycle and FP64 outer PCG on the device.
+//
+// Smoother (gauss_seidel.cu, dsType 0 "symmetric" path): partition-block Jacobi.
+// One CTA per partition keeps the partition's x in shared memory and runs the
+// inner weighted-Jacobi sweeps over in-partition couplings; cross-partition
+// couplings enter once per relax (pre: preRRSym_kernel + preAout_kernel,
+// gauss_seidel.cu:1278-2015; post: postRelaxSym_kernel, :3626-3736).  Row sums
+// run in ascending column order with separately rounded products (the reference
+// accumulates in shared-memory atomics in arbitrary order).
+//
+// PCG (CG_Flex_Cycle, cgcycle.cu:6-69) runs in FP64 on the level-0 permuted
+// numbering: b is permuted on entry and x back on exit, so the solved system is
+// A x = b (the reference applies the permuted operator to unpermuted vectors).
+// Reductions are two-stage with a fixed grid, so results are bitwise reproducible.
+#include <cmath>
+
+#include "context.cuh"
+
+namespace femgpu {
+
+namespace {
+
+constexpr int kRedBlocks = 608;  // 4 x 152 SMs: fixed grid for deterministic reductions
+constexpr int kRedThreads = 256;
+
+// device scalar slots in Ctx::red (after the partials)
+enum Slot {
+  S_BN = 0, S_NR, S_YP, S_ALPHA, S_RZ, S_RZNEW, S_ZROLD, S_BETA, S_FLAG, S_COUNT
+};
+
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (w == 0) {
+    t = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  }
+  __syncthreads();
+  return t;  // valid in thread 0
+}
+
+// ---- level kernels -----------------------------------------------------------------
+template <class T>
+__global__ void permute_in_kernel(int n, const int32_t* iperm, const T* in, T* out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = in[iperm[i]];
+}
+
+template <class T>
+__global__ void permute_out_kernel(int n, const int32_t* iperm, const T* in, T* out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[iperm[i]] = in[i];
+}
+
+template <class T>
+__global__ void cast_in_kernel(int n, const double* in, T* out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (T)in[i];
+}
+
+template <class T>
+__global__ void cast_out_kernel(int n, const T* in, double* out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (double)in[i];
+}
+
+// x += w (b - sAx - d x) / d with the weight in double (gauss_seidel.cu:1333-1341).
+template <class T>
+__device__ __forceinline__ T relax(T x, T b, T sax, T d, double w) {
+  T t = b - sax;
+  t = t - d * x;
+  return (T)((double)x + (w * (double)t) / (double)d);
+}
+
+template <class T>
+__device__ __forceinline__ T in_row_sum(const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                       const T* __restrict__ v, int row, int rs, const T* sx) {
+  T s = 0;
+  for (int e = rp[row]; e < rp[row + 1]; e++) s = s + v[e] * sx[ci[e] - rs];
+  return s;
+}
+
+// Pre-smoother of one partition: x0 = w b / d, nInner Jacobi sweeps, in-partition residual.
+template <class T>
+__global__ void pre_smooth_kernel(const int32_t* __restrict__ part_idx, const int32_t* __restrict__ agg_idx,
+                                  const int32_t* __restrict__ irp, const int32_t* __restrict__ ici,
+                                  const T* __restrict__ iv, const T* __restrict__ diag, const T* __restrict__ b,
+                                  double w, int inner, T* __restrict__ x, T* __restrict__ r) {
+  extern __shared__ unsigned char sm[];
+  const int rs = agg_idx[part_idx[blockIdx.x]], re = agg_idx[part_idx[blockIdx.x + 1]];
+  const int m = re - rs;
+  T* sx = reinterpret_cast<T*>(sm);
+  T* sax = sx + m;
+  for (int t = threadIdx.x; t < m; t += blockDim.x) {
+    int row = rs + t;
+    sx[t] = (T)((w * (double)b[row]) / (double)diag[row]);
+  }
+  __syncthreads();
+  for (int it = 0; it < inner; it++) {
+    for (int t = threadIdx.x; t < m; t += blockDim.x) sax[t] = in_row_sum(irp, ici, iv, rs + t, rs, sx);
+    __syncthreads();
+    for (int t = threadIdx.x; t < m; t += blockDim.x) {
+      int row = rs + t;
+      sx[t] = relax(sx[t], b[row], sax[t], diag[row], w);
+    }
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < m; t += blockDim.x) {
+    int row = rs + t;
+    T s = in_row_sum(irp, ici, iv, row, rs, sx);
+    T xv = sx[t];
+    x[row] = xv;
+    T u = b[row] - s;
+    r[row] = u - diag[row] * xv;
+  }
+}
+
+// r -= A_out x (preAout_kernel, gauss_seidel.cu:1977-2015).
+template <class T>
+__global__ void aout_residual_kernel(int n, const int32_t* __restrict__ orp, const int32_t* __restrict__ oci,
+                                     const T* __restrict__ ov, const T* __restrict__ x, T* __restrict__ r) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  T s = 0;
+  for (int e = orp[i]; e < orp[i + 1]; e++) s = s + ov[e] * x[oci[e]];
+  r[i] = r[i] - s;
+}
+
+// y = M x (accumulate = 0) or y = y + M x (accumulate = 1), rows summed in order.
+template <class T>
+__global__ void spmv_seq_kernel(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                const T* __restrict__ v, const T* __restrict__ x, T* __restrict__ y, int accumulate) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  T s = 0;
+  for (int e = rp[i]; e < rp[i + 1]; e++) s = s + v[e] * x[ci[e]];
+  y[i] = accumulate ? y[i] + s : s;
+}
+
+// Post-smoother relax of one partition (postRelaxSym_kernel): b' = b - A_out x, then
+// nInner Jacobi sweeps from the current x; result to xo.
+template <class T>
+__global__ void post_smooth_kernel(const int32_t* __restrict__ part_idx, const int32_t* __restrict__ agg_idx,
+                                   const int32_t* __restrict__ irp, const int32_t* __restrict__ ici,
+                                   const T* __restrict__ iv, const int32_t* __restrict__ orp,
+                                   const int32_t* __restrict__ oci, const T* __restrict__ ov,
+                                   const T* __restrict__ diag, const T* __restrict__ b, double w, int inner,
+                                   const T* __restrict__ x, T* __restrict__ xo) {
+  extern __shared__ unsigned char sm[];
+  const int rs = agg_idx[part_idx[blockIdx.x]], re = agg_idx[part_idx[blockIdx.x + 1]];
+  const int m = re - rs;
+  T* sx = reinterpret_cast<T*>(sm);
+  T* sax = sx + m;
+  T* sb = sax + m;
+  for (int t = threadIdx.x; t < m; t += blockDim.x) {
+    int row = rs + t;
+    T s = b[row];
+    for (int e = orp[row]; e < orp[row + 1]; e++) s = s + (-ov[e]) * x[oci[e]];
+    sb[t] = s;
+    sx[t] = x[row];
+  }
+  __syncthreads();
+  for (int it = 0; it < inner; it++) {
+    for (int t = threadIdx.x; t < m; t += blockDim.x) sax[t] = in_row_sum(irp, ici, iv, rs + t, rs, sx);
+    __syncthreads();
+    for (int t = threadIdx.x; t < m; t += blockDim.x) sx[t] = relax(sx[t], sb[t], sax[t], diag[rs + t], w);
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < m; t += blockDim.x) xo[rs + t] = sx[t];
+}
+
+// Coarsest level: x = A^-1 b with the explicit FP64 inverse.
+template <class T>
+__global__ void coarse_solve_kernel(int n, const double* __restrict__ inv, const T* __restrict__ b, T* __restrict__ x) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = 0.0;
+  for (int j = 0; j < n; j++) s = fma(inv[(int64_t)i * n + j], (double)b[j], s);
+  x[i] = (T)s;
+}
+
+// ---- FP64 PCG kernels -----------------------------------------------------------------
+// y = A p (rows in order, fused multiply-add) and a partial dot(y, p).
+__global__ void spmv_dot_kernel(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                const double* __restrict__ v, const double* __restrict__ p, double* __restrict__ y,
+                                double* __restrict__ partial) {
+  __shared__ double sh[32];
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int e = rp[i]; e < rp[i + 1]; e++) s = fma(v[e], p[ci[e]], s);
+    y[i] = s;
+    acc = fma(s, p[i], acc);
+  }
+  double t = block_sum(acc, sh);
+  if (threadIdx.x == 0) partial[blockIdx.x] = t;
+}
+
+__global__ void spmv_kernel(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                            const double* __restrict__ v, const double* __restrict__ x, double* __restrict__ y) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = 0.0;
+  for (int e = rp[i]; e < rp[i + 1]; e++) s = fma(v[e], x[ci[e]], s);
+  y[i] = s;
+}
+
+// partial dot(a, b) (and dot(a, c) when c != nullptr into partial2)
+__global__ void dot_kernel(int n, const double* __restrict__ a, const double* __restrict__ b,
+                           const double* __restrict__ c, double* partial, double* partial2) {
+  __shared__ double sh[32];
+  double s1 = 0.0, s2 = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    s1 = fma(a[i], b[i], s1);
+    if (c) s2 = fma(a[i], c[i], s2);
+  }
+  double t = block_sum(s1, sh);
+  if (threadIdx.x == 0) partial[blockIdx.x] = t;
+  if (c) {
+    double t2 = block_sum(s2, sh);
+    if (threadIdx.x == 0) partial2[blockIdx.x] = t2;
+  }
+}
+
+// Sum nparts partials (fixed order) into slot.
+__global__ void finalize_kernel(const double* partial, int nparts, double* slot) {
+  __shared__ double sh[32];
+  double s = 0.0;
+  for (int q = threadIdx.x; q < nparts; q += blockDim.x) s += partial[q];
+  double t = block_sum(s, sh);
+  if (threadIdx.x == 0) *slot = t;
+}
+
+// r = b - y; partial ||r||^2
+__global__ void residual_kernel(int n, const double* __restrict__ b, const double* __restrict__ y,
+                                double* __restrict__ r, double* partial) {
+  __shared__ double sh[32];
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double v = b[i] - y[i];
+    r[i] = v;
+    acc = fma(v, v, acc);
+  }
+  double t = block_sum(acc, sh);
+  if (threadIdx.x == 0) partial[blockIdx.x] = t;
+}
+
+__global__ void alpha_kernel(double* sc) {
+  double yp = sc[S_YP];
+  if (!(yp > 0.0) || !isfinite(yp)) sc[S_FLAG] = 1.0;
+  sc[S_ALPHA] = sc[S_RZ] / yp;
+}
+
+// x += alpha p; r -= alpha y (rold = r first when flexible); partial ||r||^2
+__global__ void update_kernel(int n, const double* __restrict__ sc, const double* __restrict__ p,
+                              const double* __restrict__ y, double* __restrict__ x, double* __restrict__ r,
+                              double* __restrict__ rold, double* partial) {
+  __shared__ double sh[32];
+  const double alpha = sc[S_ALPHA];
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double ri = r[i];
+    if (rold) rold[i] = ri;
+    x[i] = fma(alpha, p[i], x[i]);
+    ri = fma(-alpha, y[i], ri);
+    r[i] = ri;
+    acc = fma(ri, ri, acc);
+  }
+  double t = block_sum(acc, sh);
+  if (threadIdx.x == 0) partial[blockIdx.x] = t;
+}
+
+__global__ void beta_kernel(double* sc, int flexible) {
+  double rz = sc[S_RZ], rzn = sc[S_RZNEW];
+  sc[S_BETA] = flexible ? (rzn - sc[S_ZROLD]) / rz : rzn / rz;
+  sc[S_RZ] = rzn;
+}
+
+__global__ void pupdate_kernel(int n, const double* __restrict__ sc, const double* __restrict__ z,
+                               double* __restrict__ p) {
+  const double beta = sc[S_BETA];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = fma(beta, p[i], z[i]);
+}
+
+__global__ void copy_kernel(int n, const double* __restrict__ a, double* __restrict__ b) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = a[i];
+}
+
+__global__ void perm_vec_in_kernel(int n, const int32_t* perm, const double* in, double* out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[perm[i]] = in[i];
+}
+
+__global__ void perm_vec_out_kernel(int n, const int32_t* perm, const double* in, double* out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = in[perm[i]];
+}
+
+// ---- V-cycle driver ------------------------------------------------------------------
+template <class T>
+size_t pre_smem(const Level<T>& L) {
+  return (size_t)2 * L.max_part_rows * sizeof(T);
+}
+
+template <class T>
+int smooth_threads(const Level<T>& L) {
+  int t = ((L.max_part_rows + 31) / 32) * 32;
+  return t < 32 ? 32 : (t > 1024 ? 1024 : t);
+}
+
+template <class T>
+void set_smem_attrs(const Level<T>& L) {
+  size_t post = (size_t)3 * L.max_part_rows * sizeof(T);
+  if (post > 48 * 1024) {
+    FG_CUDA(cudaFuncSetAttribute(pre_smooth_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)post));
+    FG_CUDA(cudaFuncSetAttribute(post_smooth_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)post));
+  }
+}
+
+// b (level order for l > 0, already permuted for l == 0) -> x (same ordering).
+template <class T>
+void vcycle(Ctx& c, Hierarchy<T>& H, int l, const T* b_in, T* x_out) {
+  cudaStream_t s = c.stream;
+  Level<T>& L = *H.L[l];
+  const int n = L.A.n;
+  if (L.coarsest) {
+    FG_LAUNCH(coarse_solve_kernel<T>, grid_for(n, 128), 128, 0, s, n, L.Ainv.p, b_in, x_out);
+    return;
+  }
+  const double w = c.cfg.smootherWeight;
+  const T* b = b_in;
+  if (l > 0) {
+    FG_LAUNCH(permute_in_kernel<T>, grid_for(n, 256), 256, 0, s, n, L.iperm.p, b_in, L.b.p);
+    b = L.b.p;
+  }
+  set_smem_attrs(L);
+  const int thr = smooth_threads(L);
+  FG_LAUNCH(pre_smooth_kernel<T>, L.npart, thr, pre_smem(L), s, L.part_idx.p, L.agg_idx.p, L.Ain.rp.p, L.Ain.ci.p,
+            L.Ain.v.p, L.diag.p, b, w, c.cfg.preInnerIters, L.x.p, L.r.p);
+  FG_LAUNCH(aout_residual_kernel<T>, grid_for(n, 256), 256, 0, s, n, L.Aout.rp.p, L.Aout.ci.p, L.Aout.v.p, L.x.p,
+            L.r.p);
+  // next level: input in its t (or b when coarsest), output in its xo (or x)
+  Level<T>& N = *H.L[l + 1];
+  T* bc = N.coarsest ? N.b.p : N.t.p;
+  T* xc = N.coarsest ? N.x.p : N.xo.p;
+  FG_LAUNCH(spmv_seq_kernel<T>, grid_for(L.nagg, 128), 128, 0, s, L.nagg, L.R.rp.p, L.R.ci.p, L.R.v.p, L.r.p, bc, 0);
+  vcycle(c, H, l + 1, bc, xc);
+  FG_LAUNCH(spmv_seq_kernel<T>, grid_for(n, 128), 128, 0, s, n, L.P.rp.p, L.P.ci.p, L.P.v.p, xc, L.x.p, 1);
+  for (int rl = 0; rl < c.cfg.postRelaxes; rl++) {
+    FG_LAUNCH(post_smooth_kernel<T>, L.npart, thr, (size_t)3 * L.max_part_rows * sizeof(T), s, L.part_idx.p,
+              L.agg_idx.p, L.Ain.rp.p, L.Ain.ci.p, L.Ain.v.p, L.Aout.rp.p, L.Aout.ci.p, L.Aout.v.p, L.diag.p, b, w,
+              c.cfg.postInnerIters, L.x.p, L.r.p);
+    std::swap(L.x.p, L.r.p);  // r is free after the restriction: use it as the ping-pong buffer
+  }
+  if (l > 0) {
+    FG_LAUNCH(permute_out_kernel<T>, grid_for(n, 256), 256, 0, s, n, L.iperm.p, L.x.p, x_out);
+  } else {
+    FG_CUDA(cudaMemcpyAsync(x_out, L.x.p, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
+  }
+}
+
+// z = M r on permuted level-0 FP64 vectors.
+template <class T>
+void precondition(Ctx& c, Hierarchy<T>& H, const double* r, double* z) {
+  cudaStream_t s = c.stream;
+  Level<T>& L = *H.L[0];
+  const int n = L.A.n;
+  T* b = L.coarsest ? L.b.p : L.t.p;
+  T* x = L.coarsest ? L.x.p : L.xo.p;
+  FG_LAUNCH(cast_in_kernel<T>, grid_for(n, 256), 256, 0, s, n, r, b);
+  vcycle(c, H, 0, b, x);
+  FG_LAUNCH(cast_out_kernel<T>, grid_for(n, 256), 256, 0, s, n, x, z);
+}
+
+void precondition_any(Ctx& c, const double* r, double* z) {
+  if (c.cfg.precision == 1) precondition(c, static_cast<Hierarchy<double>&>(*c.H), r, z);
+  else precondition(c, static_cast<Hierarchy<float>&>(*c.H), r, z);
+}
+
+void ensure_work(Ctx& c, int n) {
+  cudaStream_t s = c.stream;
+  if (c.vb.n != (size_t)n) {
+    c.vb.alloc(n, s);
+    c.vx.alloc(n, s);
+    c.vr.alloc(n, s);
+    c.vz.alloc(n, s);
+    c.vp.alloc(n, s);
+    c.vy.alloc(n, s);
+    c.vrold.alloc(n, s);
+  }
+  if (c.red.n == 0) {
+    c.red.alloc(2 * kRedBlocks + 64, s);
+    c.red.zero();
+  }
+  if (!c.h_scalars) FG_CUDA(cudaMallocHost((void**)&c.h_scalars, 64 * sizeof(double)));
+}
+
+}  // namespace
+
+void spmv_original(Ctx& c, const double* d_x, double* d_y) {
+  FG_REQUIRE(c.has_matrix, FEMGPU_ERR_NOT_READY, "no operator");
+  cudaStream_t s = c.stream;
+  FG_LAUNCH(spmv_kernel, grid_for(c.A.n, 256), 256, 0, s, c.A.n, c.A.rp.p, c.A.ci.p, c.A.v.p, d_x, d_y);
+}
+
+void amg_vcycle_device(Ctx& c, const double* d_r, double* d_z) {
+  FG_REQUIRE(c.has_hierarchy, FEMGPU_ERR_NOT_READY, "call femgpu_setup first");
+  const int n = c.A.n;
+  cudaStream_t s = c.stream;
+  ensure_work(c, n);
+  FG_LAUNCH(perm_vec_in_kernel, grid_for(n, 256), 256, 0, s, n, c.perm0.p, d_r, c.vr.p);
+  precondition_any(c, c.vr.p, c.vz.p);
+  FG_LAUNCH(perm_vec_out_kernel, grid_for(n, 256), 256, 0, s, n, c.perm0.p, c.vz.p, d_z);
+}
+
+SolveResult amg_solve_device(Ctx& c, const double* d_b, double* d_x) {
+  FG_REQUIRE(c.has_hierarchy, FEMGPU_ERR_NOT_READY, "call femgpu_setup first");
+  const int n = c.A.n;
+  cudaStream_t s = c.stream;
+  ensure_work(c, n);
+  SolveResult res;
+  double* part = c.red.p;
+  double* part2 = c.red.p + kRedBlocks;
+  double* sc = c.red.p + 2 * kRedBlocks;
+  const DCsr<double>& A = c.A0p;
+  FG_LAUNCH(perm_vec_in_kernel, grid_for(n, 256), 256, 0, s, n, c.perm0.p, d_b, c.vb.p);
+  FG_LAUNCH(perm_vec_in_kernel, grid_for(n, 256), 256, 0, s, n, c.perm0.p, d_x, c.vx.p);
+  if (c.cfg.solverType == 0) {
+    // AMG_SOLVER: one V-cycle applied to b (amg.cu:150-160); x is overwritten
+    precondition_any(c, c.vb.p, c.vx.p);
+    FG_LAUNCH(perm_vec_out_kernel, grid_for(n, 256), 256, 0, s, n, c.perm0.p, c.vx.p, d_x);
+    FG_LAUNCH(spmv_kernel, grid_for(n, 256), 256, 0, s, n, A.rp.p, A.ci.p, A.v.p, c.vx.p, c.vy.p);
+    FG_LAUNCH(residual_kernel, kRedBlocks, kRedThreads, 0, s, n, c.vb.p, c.vy.p, c.vr.p, part);
+    FG_LAUNCH(finalize_kernel, 1, 1024, 0, s, part, kRedBlocks, sc + S_NR);
+    FG_LAUNCH(dot_kernel, kRedBlocks, kRedThreads, 0, s, n, c.vb.p, c.vb.p, nullptr, part, nullptr);
+    FG_LAUNCH(finalize_kernel, 1, 1024, 0, s, part, kRedBlocks, sc + S_BN);
+    FG_CUDA(cudaMemcpyAsync(c.h_scalars, sc, S_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s));
+    FG_CUDA(cudaStreamSynchronize(s));
+    double bn = sqrt(c.h_scalars[S_BN]);
+    res.relres = sqrt(c.h_scalars[S_NR]) / (bn > 0 ? bn : 1.0);
+    res.iterations = 1;
+    return res;
+  }
+  const int flexible = c.cfg.flexibleCG;
+  FG_LAUNCH(dot_kernel, kRedBlocks, kRedThreads, 0, s, n, c.vb.p, c.vb.p, nullptr, part, nullptr);
+  FG_LAUNCH(finalize_kernel, 1, 1024, 0, s, part, kRedBlocks, sc + S_BN);
+  FG_LAUNCH(spmv_kernel, grid_for(n, 256), 256, 0, s, n, A.rp.p, A.ci.p, A.v.p, c.vx.p, c.vy.p);
+  FG_LAUNCH(residual_kernel, kRedBlocks, kRedThreads, 0, s, n, c.vb.p, c.vy.p, c.vr.p, part);
+  FG_LAUNCH(finalize_kernel, 1, 1024, 0, s, part, kRedBlocks, sc + S_NR);
+  FG_CUDA(cudaMemsetAsync(sc + S_FLAG, 0, sizeof(double), s));
+  FG_CUDA(cudaMemcpyAsync(c.h_scalars, sc, S_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s));
+  FG_CUDA(cudaStreamSynchronize(s));
+  double bnorm = sqrt(c.h_scalars[S_BN]);
+  if (bnorm == 0.0) bnorm = 1.0;
+  double nr = sqrt(c.h_scalars[S_NR]);
+  const double tol = c.cfg.tolerance;
+  int it = 0;
+  res.status = FEMGPU_ERR_NOT_CONVERGED;
+  if (nr / bnorm <= tol) {
+    res.status = FEMGPU_OK;
+  } else {
+    precondition_any(c, c.vr.p, c.vz.p);
+    FG_LAUNCH(copy_kernel, kRedBlocks, kRedThreads, 0, s, n, c.vz.p, c.vp.p);
+    FG_LAUNCH(dot_kernel, kRedBlocks, kRedThreads, 0, s, n, c.vr.p, c.vz.p, nullptr, part, nullptr);
+    FG_LAUNCH(finalize_kernel, 1, 1024, 0, s, part, kRedBlocks, sc + S_RZ);
+    while (it < c.cfg.maxIters) {
+      FG_LAUNCH(spmv_dot_kernel, kRedBlocks, kRedThreads, 0, s, n, A.rp.p, A.ci.p, A.v.p, c.vp.p, c.vy.p, part);
+      FG_LAUNCH(finalize_kernel, 1, 1024, 0, s, part, kRedBlocks, sc + S_YP);
+      FG_LAUNCH(alpha_kernel, 1, 1, 0, s, sc);
+      FG_LAUNCH(update_kernel, kRedBlocks, kRedThreads, 0, s, n, sc, c.vp.p, c.vy.p, c.vx.p, c.vr.p,
+                flexible ? c.vrold.p : nullptr, part);
+      FG_LAUNCH(finalize_kernel, 1, 1024, 0, s, part, kRedBlocks, sc + S_NR);
+      FG_CUDA(cudaMemcpyAsync(c.h_scalars, sc, S_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s));
+      FG_CUDA(cudaStreamSynchronize(s));
+      it++;
+      nr = sqrt(c.h_scalars[S_NR]);
+      if (c.h_scalars[S_FLAG] != 0.0 || !std::isfinite(nr)) {
+        res.status = FEMGPU_ERR_BREAKDOWN;
+        break;
+      }
+      if (nr / bnorm <= tol) {
+        res.status = FEMGPU_OK;
+        break;
+      }
+      precondition_any(c, c.vr.p, c.vz.p);
+      FG_LAUNCH(dot_kernel, kRedBlocks, kRedThreads, 0, s, n, c.vz.p, c.vr.p, flexible ? c.vrold.p : nullptr, part,
+                part2);
+      FG_LAUNCH(finalize_kernel, 1, 1024, 0, s, part, kRedBlocks, sc + S_RZNEW);
+      if (flexible) FG_LAUNCH(finalize_kernel, 1, 1024, 0, s, part2, kRedBlocks, sc + S_ZROLD);
+      FG_LAUNCH(beta_kernel, 1, 1, 0, s, sc, flexible);
+      FG_LAUNCH(pupdate_kernel, kRedBlocks, kRedThreads, 0, s, n, sc, c.vz.p, c.vp.p);
+    }
+  }
+  FG_LAUNCH(perm_vec_out_kernel, grid_for(n, 256), 256, 0, s, n, c.perm0.p, c.vx.p, d_x);
+  res.iterations = it;
+  res.relres = nr / bnorm;
+  return res;
+}
+
+}  // namespace femgpu

@@ -1,0 +1,187 @@
+// common.cuh -- shared device infrastructure of libfemgpu (sm_103a).
+//
+// Conventions used by every kernel file:
+//  * all work runs on the handle's stream; device memory comes from
+//    cudaMallocAsync on that stream (stream-ordered, no device-wide syncs);
+//  * the library is compiled with -fmad=false: no multiply-add is fused unless
+//    the source says fma()/fmaf(), so rounding matches the CPU oracle exactly;
+//  * every loop that waits for a convergence flag has an iteration cap and
+//    reports FEMGPU_ERR_LIMIT instead of spinning forever.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/femgpu.h"
+
+namespace femgpu {
+
+struct Error : std::runtime_error {
+  femgpu_status status;
+  Error(femgpu_status s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+#define FG_CUDA(call)                                                                        \
+  do {                                                                                       \
+    cudaError_t e_ = (call);                                                                 \
+    if (e_ != cudaSuccess)                                                                   \
+      throw ::femgpu::Error(FEMGPU_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+#define FG_CHECK_LAUNCH() FG_CUDA(cudaGetLastError())
+
+#define FG_REQUIRE(cond, status, msg)                     \
+  do {                                                    \
+    if (!(cond)) throw ::femgpu::Error((status), (msg));  \
+  } while (0)
+
+// Stream-ordered device buffer.
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaStream_t s = 0;
+  DBuf() = default;
+  DBuf(size_t count, cudaStream_t st) { alloc(count, st); }
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  DBuf(DBuf&& o) noexcept : p(o.p), n(o.n), s(o.s) { o.p = nullptr; o.n = 0; }
+  DBuf& operator=(DBuf&& o) noexcept {
+    if (this != &o) {
+      release();
+      p = o.p; n = o.n; s = o.s;
+      o.p = nullptr; o.n = 0;
+    }
+    return *this;
+  }
+  ~DBuf() { release(); }
+  void alloc(size_t count, cudaStream_t st) {
+    release();
+    s = st;
+    n = count;
+    if (count) {
+      cudaError_t e = cudaMallocAsync((void**)&p, count * sizeof(T), st);
+      if (e != cudaSuccess) {
+        p = nullptr;
+        n = 0;
+        (void)cudaGetLastError();
+        throw Error(FEMGPU_ERR_ALLOC, std::string("cudaMallocAsync: ") + cudaGetErrorString(e));
+      }
+    }
+  }
+  void release() {
+    if (p) cudaFreeAsync(p, s);
+    p = nullptr;
+    n = 0;
+  }
+  void zero() {
+    if (n) FG_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), s));
+  }
+  void upload(const T* h, size_t count) {
+    FG_REQUIRE(count <= n, FEMGPU_ERR_INVALID, "upload larger than buffer");
+    if (count) FG_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+  }
+  void download(T* h, size_t count) const {
+    FG_REQUIRE(count <= n, FEMGPU_ERR_INVALID, "download larger than buffer");
+    if (count) FG_CUDA(cudaMemcpyAsync(h, p, count * sizeof(T), cudaMemcpyDeviceToHost, s));
+  }
+  std::vector<T> to_host() const {
+    std::vector<T> v(n);
+    download(v.data(), n);
+    FG_CUDA(cudaStreamSynchronize(s));
+    return v;
+  }
+};
+
+// CSR matrix in device memory.
+template <class T>
+struct DCsr {
+  int n = 0, m = 0;
+  int64_t nnz = 0;
+  DBuf<int32_t> rp, ci;
+  DBuf<T> v;
+};
+
+inline int grid_for(int64_t n, int block) {
+  int64_t g = (n + block - 1) / block;
+  if (g < 1) g = 1;
+  if (g > 2147483647LL) g = 2147483647LL;
+  return (int)g;
+}
+
+// Reads one device scalar synchronously (used only at setup-time loop checks).
+template <class T>
+inline T read_scalar(const T* d, cudaStream_t s) {
+  T h;
+  FG_CUDA(cudaMemcpyAsync(&h, d, sizeof(T), cudaMemcpyDeviceToHost, s));
+  FG_CUDA(cudaStreamSynchronize(s));
+  return h;
+}
+
+// ---- device primitives (primitives.cu) --------------------------------------
+// Exclusive scan of n int32 counts into out[0..n] (out[n] = total, int64 safe
+// total returned).  out may alias in only if in has n+1 entries.
+int64_t exclusive_scan(const int32_t* in, int32_t* out, int64_t n, cudaStream_t s);
+// Inclusive scan in place.
+void inclusive_scan_inplace(int32_t* a, int64_t n, cudaStream_t s);
+int32_t reduce_max(const int32_t* a, int64_t n, cudaStream_t s);
+int64_t count_equal(const int32_t* a, int64_t n, int32_t value, cudaStream_t s);
+void fill_i32(int32_t* a, int64_t n, int32_t v, cudaStream_t s);
+void iota_i32(int32_t* a, int64_t n, cudaStream_t s);
+// Segmented in-place ascending sort of int32 values; segment k spans
+// [off[k], off[k+1]).  With unique != nullptr each segment is also deduplicated
+// in place and its unique length written to unique[k].
+void segmented_sort_i32(int32_t* vals, const int32_t* off, int nseg, int32_t* unique_counts, cudaStream_t s);
+
+// ---- small device helpers -----------------------------------------------------
+__device__ __forceinline__ int lower_bound_i32(const int32_t* a, int lo, int hi, int key) {
+  // first index in [lo, hi) with a[i] >= key
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (a[mid] < key) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Bitonic sort of n (power of two) keys in shared memory by the threads
+// [t0, t0 + nthreads) that call it; sync() is __syncwarp or __syncthreads.
+template <class K, class Sync>
+__device__ __forceinline__ void bitonic_sort_shared(K* s, int n, int tid, int nthreads, Sync sync) {
+  for (int size = 2; size <= n; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int i = tid; i < (n >> 1); i += nthreads) {
+        int lo = 2 * i - (i & (stride - 1));
+        int hi = lo + stride;
+        bool asc = (lo & size) == 0;
+        K a = s[lo], b = s[hi];
+        if ((a > b) == asc) {
+          s[lo] = b;
+          s[hi] = a;
+        }
+      }
+      sync();
+    }
+  }
+}
+
+struct WarpSync {
+  __device__ void operator()() const { __syncwarp(); }
+};
+struct BlockSync {
+  __device__ void operator()() const { __syncthreads(); }
+};
+
+__host__ __device__ inline int next_pow2(int v) {
+  int p = 1;
+  while (p < v) p <<= 1;
+  return p;
+}
+
+}  // namespace femgpu

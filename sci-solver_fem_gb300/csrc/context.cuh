@@ -1,0 +1,116 @@
+// context.cuh -- solver context (one per femgpu_handle) and the AMG level layout.
+//
+// Device layout of one level (all arrays in HBM, indices int32):
+//   A      CSR of the level operator in the level's own numbering (T values);
+//   perm   old -> new row id (aggregate-contiguous, partition-contiguous order);
+//   Ap     CSR of perm(A) with sorted columns;
+//   diag   diagonal of Ap;
+//   Ain    per row: in-partition off-diagonal entries (upper value mirrored);
+//   Aout   per row: cross-partition entries;
+//   P, R   prolongator (n x n_agg) and its transpose;
+//   agg_idx / part_idx   aggregate offsets over new rows, partition offsets over aggregates.
+// The coarsest level keeps the explicit inverse of its dense matrix (FP64).
+#pragma once
+
+#include <atomic>
+#include <memory>
+#include <string>
+
+#include "common.cuh"
+
+namespace femgpu {
+
+extern std::atomic<int64_t> g_kernel_launches;
+
+#define FG_LAUNCH(kernel, grid, block, smem, stream, ...)                     \
+  do {                                                                        \
+    ::femgpu::g_kernel_launches.fetch_add(1, std::memory_order_relaxed);      \
+    kernel<<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);               \
+    FG_CHECK_LAUNCH();                                                        \
+  } while (0)
+
+struct Mesh {
+  int dim = 0, k = 0;
+  int64_t nv = 0, ne = 0;
+  bool has_labels = false;
+  DBuf<double> xyz;       // nv x 3
+  DBuf<int32_t> conn;     // ne x k
+  DBuf<int32_t> labels;   // ne
+  DBuf<int32_t> vstart;   // nv + 1: incidence offsets
+  DBuf<int32_t> inc;      // ne * k: e * k + a, sorted per vertex
+};
+
+template <class T>
+struct Level {
+  int n = 0, nagg = 0, npart = 0;
+  bool coarsest = false;
+  DCsr<T> A;
+  DBuf<int32_t> gxadj, gadj;  // aggregation graph of this level
+  int64_t gnnz = 0;
+  DBuf<int32_t> perm, iperm, agg_idx, part_idx, agg_of;
+  DCsr<T> Ap, Ain, Aout, P, R;
+  DBuf<T> diag;
+  int max_part_rows = 0;
+  // coarsest: explicit inverse, row-major n x n
+  DBuf<double> Ainv;
+  // work vectors (level numbering / permuted numbering)
+  DBuf<T> b, x, r, xo, t;
+};
+
+struct HierarchyBase {
+  virtual ~HierarchyBase() {}
+  int num_levels = 0;
+};
+
+template <class T>
+struct Hierarchy : HierarchyBase {
+  std::vector<std::unique_ptr<Level<T>>> L;
+};
+
+struct Ctx {
+  femgpu_config cfg{};
+  int device = 0;
+  cudaStream_t stream = 0;
+  bool own_stream = false;
+  std::string last_error;
+
+  Mesh mesh;
+  bool has_mesh = false;
+  DCsr<double> A;                // level-0 operator, original numbering, FP64
+  DBuf<int32_t> gxadj, gadj;     // level-0 aggregation graph
+  int64_t graph_nnz = 0;
+  bool has_matrix = false;
+
+  // hierarchy (built by femgpu_setup)
+  std::unique_ptr<HierarchyBase> H;
+  DBuf<int32_t> perm0;           // level-0 old -> new (identity if level 0 is the coarsest)
+  DCsr<double> A0p;              // FP64 level-0 operator in permuted order (outer PCG)
+  bool has_hierarchy = false;
+  double setup_ms = 0.0;
+
+  // PCG work vectors (permuted order)
+  DBuf<double> vb, vx, vr, vz, vp, vy, vrold;
+  DBuf<double> red;              // reduction partials + scalars
+  double* h_scalars = nullptr;   // pinned host mirror of the device scalars
+};
+
+// fem_assembly.cu
+void build_mesh_pattern(Ctx& c);
+void assemble_operator(Ctx& c, const double* coef_host, double lambda);
+void load_vector(Ctx& c, const double* f_host, double* b_host);
+void apply_dirichlet(Ctx& c, const uint8_t* mask_host);
+
+// amg_setup.cu
+void amg_setup(Ctx& c);
+
+// amg_solve.cu
+struct SolveResult {
+  int iterations = 0;
+  double relres = 0.0;
+  femgpu_status status = FEMGPU_OK;
+};
+SolveResult amg_solve_device(Ctx& c, const double* d_b, double* d_x);
+void amg_vcycle_device(Ctx& c, const double* d_r, double* d_z);
+void spmv_original(Ctx& c, const double* d_x, double* d_y);
+
+}  // namespace femgpu
