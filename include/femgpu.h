@@ -88,6 +88,10 @@ void femgpu_config_default(femgpu_config* cfg);
  * (src/FEMSolver.cu:99-129), which the reference never calls. */
 femgpu_status femgpu_create(femgpu_handle* h, const femgpu_config* cfg);
 femgpu_status femgpu_destroy(femgpu_handle h);
+/* Replaces the options of an existing context (device and stream stay); the next
+ * femgpu_setup uses them.  The reference reads its option members when solveFEM
+ * constructs the AMG object (src/FEMSolver.cu:66-73). */
+femgpu_status femgpu_set_config(femgpu_handle h, const femgpu_config* cfg);
 const char* femgpu_status_string(femgpu_status s);
 /* Last error message recorded on this handle (empty string if none). */
 const char* femgpu_last_error(femgpu_handle h);

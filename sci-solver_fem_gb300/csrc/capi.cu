@@ -211,6 +211,27 @@ femgpu_status femgpu_destroy(femgpu_handle h) {
   return FEMGPU_OK;
 }
 
+femgpu_status femgpu_set_config(femgpu_handle h, const femgpu_config* cfg) {
+  if (!h || !cfg) return FEMGPU_ERR_INVALID;
+  return guard(h, [&] {
+    FG_REQUIRE(cfg->maxLevels >= 1 && cfg->topSize >= 1 && cfg->maxIters >= 0, FEMGPU_ERR_INVALID,
+               "maxLevels, topSize must be >= 1 and maxIters >= 0");
+    FG_REQUIRE(cfg->partitionMaxSize >= 1 && cfg->preInnerIters >= 0 && cfg->postInnerIters >= 0 &&
+                   cfg->postRelaxes >= 0,
+               FEMGPU_ERR_INVALID, "invalid smoother options");
+    FG_REQUIRE(cfg->precision == 0 || cfg->precision == 1, FEMGPU_ERR_INVALID, "precision must be 0 or 1");
+    femgpu_config c = *cfg;
+    c.device = h->cfg.device;
+    c.stream = h->cfg.stream;
+    bool rebuild = c.precision != h->cfg.precision || c.seed != h->cfg.seed || c.maxLevels != h->cfg.maxLevels ||
+                   c.topSize != h->cfg.topSize || c.randMisParameters != h->cfg.randMisParameters ||
+                   c.partitionMaxSize != h->cfg.partitionMaxSize || c.proOmega != h->cfg.proOmega ||
+                   c.aggregatorType != h->cfg.aggregatorType;
+    h->cfg = c;
+    if (rebuild) invalidate_hierarchy(*h);
+  });
+}
+
 femgpu_status femgpu_set_mesh(femgpu_handle h, int dim, int64_t nverts, const double* xyz, int64_t nelems,
                               const int32_t* conn, const int32_t* labels) {
   if (!h) return FEMGPU_ERR_INVALID;

@@ -20,7 +20,8 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "not ready", 4: "b
 
 # every symbol include/femgpu.h declares
 EXPORTS = [
-    "femgpu_config_default", "femgpu_create", "femgpu_destroy", "femgpu_status_string", "femgpu_last_error",
+    "femgpu_config_default", "femgpu_create", "femgpu_destroy", "femgpu_set_config", "femgpu_status_string",
+    "femgpu_last_error",
     "femgpu_set_mesh", "femgpu_assemble", "femgpu_load_vector", "femgpu_set_dirichlet", "femgpu_set_matrix_csr",
     "femgpu_setup", "femgpu_solve", "femgpu_solve_device", "femgpu_spmv_device", "femgpu_get_matrix",
     "femgpu_num_levels", "femgpu_get_level_info", "femgpu_level_get", "femgpu_vcycle", "femgpu_kernel_launches",
@@ -79,6 +80,7 @@ def lib():
     L.femgpu_config_default.restype = None
     L.femgpu_create.argtypes = [C.POINTER(_vp), C.POINTER(Config)]
     L.femgpu_destroy.argtypes = [_vp]
+    L.femgpu_set_config.argtypes = [_vp, C.POINTER(Config)]
     L.femgpu_status_string.argtypes = [C.c_int]
     L.femgpu_status_string.restype = C.c_char_p
     L.femgpu_last_error.argtypes = [_vp]
