@@ -694,13 +694,10 @@ __global__ void esc_count_items_kernel(EscArgs<T> a) {
   if (i < a.n) a.counts[i] = esc_row_items<T, MODE>(a, i);
 }
 
-__global__ void collect_big_rows_kernel(int n, const int32_t* items, int cap, int32_t* list, int32_t* nlist,
-                                        int32_t* overflow, int hard_cap) {
+__global__ void collect_big_rows_kernel(int n, const int32_t* items, int cap, int hard_cap, int32_t* list,
+                                        int32_t* nlist) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n && items[i] > cap) {
-    if (items[i] > hard_cap) atomicExch(overflow, 1);
-    else list[atomicAdd(nlist, 1)] = i;
-  }
+  if (i < n && items[i] > cap && items[i] <= hard_cap) list[atomicAdd(nlist, 1)] = i;
 }
 
 template <class T, int MODE, bool WRITE>
@@ -751,21 +748,124 @@ __global__ void esc_block_kernel(EscArgs<T> a, const int32_t* items) {
   }
 }
 
+// Rows beyond the shared-memory sort capacity (they appear only on coarse levels,
+// where the column count is small): one block per row, a dense accumulator over
+// the output columns; thread 0 walks the items in generation order (so every
+// column is summed left to right from its first item), then the block compacts
+// the touched columns in ascending order.
+template <class T, int MODE>
+__device__ void esc_dense_row(const EscArgs<T>& a, int i, T* acc, unsigned char* mark, int ncols) {
+  auto add = [&](int col, T v) {
+    if (!mark[col]) {
+      mark[col] = 1;
+      acc[col] = v;
+    } else {
+      acc[col] = acc[col] + v;
+    }
+  };
+  int r = esc_input_row<T, MODE>(a, i);
+  int b = a.arp[r], e = a.arp[r + 1];
+  for (int q = b; q < e; q++) {
+    int j = a.aci[q];
+    if (MODE == ESC_PERMUTE) {
+      add(a.perm ? a.perm[j] : j, a.av[q]);
+    } else if (MODE == ESC_PROLONG) {
+      T t = (a.neg_omega * a.av[q]) * (T)1;
+      add(a.agg_of[j], t / a.diag[i]);
+    } else {
+      T av = a.av[q];
+      for (int f = a.brp[j]; f < a.brp[j + 1]; f++) add(a.bci[f], av * a.bv[f]);
+    }
+  }
+  if (MODE == ESC_PROLONG) add(a.agg_of[i], (T)1);
+}
+
+template <class T, int MODE, bool WRITE>
+__global__ void esc_dense_kernel(EscArgs<T> a, int ncols, T* gacc, unsigned char* gmark) {
+  extern __shared__ unsigned char smem_raw[];
+  const bool shared = gacc == nullptr;
+  __shared__ int s_total;
+  __shared__ int s_warp[32];
+  for (int bi = blockIdx.x; bi < a.nbig; bi += gridDim.x) {
+    int i = a.big_rows[bi];
+    T* acc = shared ? reinterpret_cast<T*>(smem_raw) : gacc + (size_t)blockIdx.x * ncols;
+    unsigned char* mark = shared ? smem_raw + (size_t)ncols * sizeof(T) : gmark + (size_t)blockIdx.x * ncols;
+    for (int q = threadIdx.x; q < ncols; q += blockDim.x) mark[q] = 0;
+    __syncthreads();
+    if (threadIdx.x == 0) esc_dense_row<T, MODE>(a, i, acc, mark, ncols);
+    __syncthreads();
+    // ordered compaction of marked columns
+    int base = 0;
+    int out = WRITE ? a.orp[i] : 0;
+    for (int c0 = 0; c0 < ncols; c0 += blockDim.x) {
+      int q = c0 + threadIdx.x;
+      int m = (q < ncols && mark[q]) ? 1 : 0;
+      unsigned bal = __ballot_sync(0xffffffffu, m);
+      int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+      if (lane == 0) s_warp[w] = __popc(bal);
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        int t = 0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) {
+          int v = s_warp[k];
+          s_warp[k] = t;
+          t += v;
+        }
+        s_total = t;
+      }
+      __syncthreads();
+      if (m && WRITE) {
+        int pos = base + s_warp[w] + __popc(bal & ((1u << lane) - 1u));
+        a.oci[out + pos] = q;
+        a.ov[out + pos] = acc[q];
+      }
+      base += s_total;
+      __syncthreads();
+    }
+    if (!WRITE && threadIdx.x == 0) a.counts[i] = base;
+    __syncthreads();
+  }
+}
+
+__global__ void collect_dense_rows_kernel(int n, const int32_t* items, int cap, int32_t* list, int32_t* nlist) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && items[i] > cap) list[atomicAdd(nlist, 1)] = i;
+}
+
 template <class T, int MODE>
 void run_esc(Ctx& c, EscArgs<T> a, int nrows_out, int ncols_out, DCsr<T>& out) {
   cudaStream_t s = c.stream;
   a.n = nrows_out;
-  DBuf<int32_t> items(nrows_out + 1, s), ucnt(nrows_out + 1, s), big(nrows_out + 1, s), nbig(1, s), ovf(1, s);
+  DBuf<int32_t> items(nrows_out + 1, s), ucnt(nrows_out + 1, s), big(nrows_out + 1, s), nbig(1, s);
+  DBuf<int32_t> dense(nrows_out + 1, s), ndense(1, s);
   nbig.zero();
-  ovf.zero();
+  ndense.zero();
   a.counts = items.p;
   FG_LAUNCH((esc_count_items_kernel<T, MODE>), grid_for(nrows_out, 256), 256, 0, s, a);
-  FG_LAUNCH(collect_big_rows_kernel, grid_for(nrows_out, 256), 256, 0, s, nrows_out, items.p, kEscWarpCap, big.p,
-            nbig.p, ovf.p, kEscBlockCap);
-  FG_REQUIRE(read_scalar(ovf.p, s) == 0, FEMGPU_ERR_LIMIT,
-             "a sparse row has more than 8192 products (row-wise SpGEMM capacity)");
+  FG_LAUNCH(collect_big_rows_kernel, grid_for(nrows_out, 256), 256, 0, s, nrows_out, items.p, kEscWarpCap,
+            kEscBlockCap, big.p, nbig.p);
+  FG_LAUNCH(collect_dense_rows_kernel, grid_for(nrows_out, 256), 256, 0, s, nrows_out, items.p, kEscBlockCap,
+            dense.p, ndense.p);
   a.nbig = read_scalar(nbig.p, s);
   a.big_rows = big.p;
+  EscArgs<T> ad = a;  // dense tier: rows with more items than the sort capacity
+  ad.nbig = read_scalar(ndense.p, s);
+  ad.big_rows = dense.p;
+  const int dgrid = std::min(ad.nbig, 152 * 2);
+  const size_t dsm = (size_t)ncols_out * (sizeof(T) + 1);
+  const bool dense_shared = dsm <= 200 * 1024;
+  DBuf<T> gacc;
+  DBuf<unsigned char> gmark;
+  if (ad.nbig > 0 && !dense_shared) {
+    FG_REQUIRE((size_t)dgrid * ncols_out * (sizeof(T) + 1) <= ((size_t)8 << 30), FEMGPU_ERR_LIMIT,
+               "dense accumulator for long SpGEMM rows exceeds 8 GB");
+    gacc.alloc((size_t)dgrid * ncols_out, s);
+    gmark.alloc((size_t)dgrid * ncols_out, s);
+  }
+  if (ad.nbig > 0 && dense_shared && dsm > 48 * 1024) {
+    FG_CUDA(cudaFuncSetAttribute(esc_dense_kernel<T, MODE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm));
+    FG_CUDA(cudaFuncSetAttribute(esc_dense_kernel<T, MODE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm));
+  }
   const size_t wsm = (size_t)kEscWarps * kEscWarpCap * (sizeof(unsigned long long) + sizeof(T));
   const size_t bsm = (size_t)kEscBlockCap * (sizeof(unsigned long long) + sizeof(T));
   static bool attr_set = false;
@@ -781,6 +881,11 @@ void run_esc(Ctx& c, EscArgs<T> a, int nrows_out, int ncols_out, DCsr<T>& out) {
   FG_LAUNCH((esc_warp_kernel<T, MODE, false>), wgrid, 32 * kEscWarps, wsm, s, a, items.p);
   if (a.nbig > 0)
     FG_LAUNCH((esc_block_kernel<T, MODE, false>), std::min(a.nbig, 152 * 2), kEscBlockThreads, bsm, s, a, items.p);
+  if (ad.nbig > 0) {
+    ad.counts = ucnt.p;
+    FG_LAUNCH((esc_dense_kernel<T, MODE, false>), dgrid, 256, dense_shared ? dsm : 0, s, ad, ncols_out, gacc.p,
+              gmark.p);
+  }
   out.n = nrows_out;
   out.m = ncols_out;
   out.rp.alloc(nrows_out + 1, s);
@@ -793,6 +898,13 @@ void run_esc(Ctx& c, EscArgs<T> a, int nrows_out, int ncols_out, DCsr<T>& out) {
   FG_LAUNCH((esc_warp_kernel<T, MODE, true>), wgrid, 32 * kEscWarps, wsm, s, a, items.p);
   if (a.nbig > 0)
     FG_LAUNCH((esc_block_kernel<T, MODE, true>), std::min(a.nbig, 152 * 2), kEscBlockThreads, bsm, s, a, items.p);
+  if (ad.nbig > 0) {
+    ad.orp = out.rp.p;
+    ad.oci = out.ci.p;
+    ad.ov = out.v.p;
+    FG_LAUNCH((esc_dense_kernel<T, MODE, true>), dgrid, 256, dense_shared ? dsm : 0, s, ad, ncols_out, gacc.p,
+              gmark.p);
+  }
 }
 
 // ---- level matrices -----------------------------------------------------------------
@@ -1176,6 +1288,7 @@ void amg_setup(Ctx& c) {
   cudaEventDestroy(e1);
   c.setup_ms = ms;
   c.has_hierarchy = true;
+  c.hier_gen++;  // invalidates the captured PCG iteration graph
 }
 
 }  // namespace femgpu

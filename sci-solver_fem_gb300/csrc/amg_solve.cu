@@ -25,7 +25,7 @@ constexpr int kRedThreads = 256;
 
 // device scalar slots in Ctx::red (after the partials)
 enum Slot {
-  S_BN = 0, S_NR, S_YP, S_ALPHA, S_RZ, S_RZNEW, S_ZROLD, S_BETA, S_FLAG, S_COUNT
+  S_BN = 0, S_NR, S_YP, S_ALPHA, S_RZ, S_RZNEW, S_ZROLD, S_BETA, S_FLAG, S_FIRST, S_COUNT
 };
 
 __device__ __forceinline__ double block_sum(double v, double* sh) {
@@ -275,11 +275,20 @@ __global__ void update_kernel(int n, const double* __restrict__ sc, const double
   if (threadIdx.x == 0) partial[blockIdx.x] = t;
 }
 
+// beta (cgcycle.cu:52-54; Polak-Ribiere when flexible); 0 on the first iteration,
+// where p = z.
 __global__ void beta_kernel(double* sc, int flexible) {
   double rz = sc[S_RZ], rzn = sc[S_RZNEW];
-  sc[S_BETA] = flexible ? (rzn - sc[S_ZROLD]) / rz : rzn / rz;
+  if (sc[S_FIRST] != 0.0) {
+    sc[S_BETA] = 0.0;
+    sc[S_FIRST] = 0.0;
+  } else {
+    sc[S_BETA] = flexible ? (rzn - sc[S_ZROLD]) / rz : rzn / rz;
+  }
   sc[S_RZ] = rzn;
 }
+
+__global__ void set_slot_kernel(double* sc, int slot, double v) { sc[slot] = v; }
 
 __global__ void pupdate_kernel(int n, const double* __restrict__ sc, const double* __restrict__ z,
                                double* __restrict__ p) {
@@ -418,14 +427,92 @@ void amg_vcycle_device(Ctx& c, const double* d_r, double* d_z) {
   FG_LAUNCH(perm_vec_out_kernel, grid_for(n, 256), 256, 0, s, n, c.perm0.p, c.vz.p, d_z);
 }
 
+namespace {
+
+// One PCG iteration after the residual check: z = M r, beta, p = z + beta p,
+// y = A p, alpha, x += alpha p, r -= alpha y, ||r||^2, scalars to the host.
+void pcg_iteration_body(Ctx& c, int n, int flexible) {
+  cudaStream_t s = c.stream;
+  double* part = c.red.p;
+  double* part2 = c.red.p + kRedBlocks;
+  double* sc = c.red.p + 2 * kRedBlocks;
+  const DCsr<double>& A = c.A0p;
+  precondition_any(c, c.vr.p, c.vz.p);
+  FG_LAUNCH(dot_kernel, kRedBlocks, kRedThreads, 0, s, n, c.vz.p, c.vr.p, flexible ? c.vrold.p : nullptr, part,
+            part2);
+  FG_LAUNCH(finalize_kernel, 1, 1024, 0, s, part, kRedBlocks, sc + S_RZNEW);
+  if (flexible) FG_LAUNCH(finalize_kernel, 1, 1024, 0, s, part2, kRedBlocks, sc + S_ZROLD);
+  FG_LAUNCH(beta_kernel, 1, 1, 0, s, sc, flexible);
+  FG_LAUNCH(pupdate_kernel, kRedBlocks, kRedThreads, 0, s, n, sc, c.vz.p, c.vp.p);
+  FG_LAUNCH(spmv_dot_kernel, kRedBlocks, kRedThreads, 0, s, n, A.rp.p, A.ci.p, A.v.p, c.vp.p, c.vy.p, part);
+  FG_LAUNCH(finalize_kernel, 1, 1024, 0, s, part, kRedBlocks, sc + S_YP);
+  FG_LAUNCH(alpha_kernel, 1, 1, 0, s, sc);
+  FG_LAUNCH(update_kernel, kRedBlocks, kRedThreads, 0, s, n, sc, c.vp.p, c.vy.p, c.vx.p, c.vr.p,
+            flexible ? c.vrold.p : nullptr, part);
+  FG_LAUNCH(finalize_kernel, 1, 1024, 0, s, part, kRedBlocks, sc + S_NR);
+  FG_CUDA(cudaMemcpyAsync(c.h_scalars, sc, S_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s));
+}
+
+// Captures the iteration body once per hierarchy as a CUDA graph.
+bool capture_iteration(Ctx& c, int n, int flexible) {
+  if (c.pcg_exec && c.graph_gen == c.hier_gen && c.graph_flexible == flexible) return true;
+  if (c.pcg_exec) {
+    cudaGraphExecDestroy(c.pcg_exec);
+    c.pcg_exec = nullptr;
+  }
+  cudaStream_t s = c.stream;
+  int64_t before = g_kernel_launches.load();
+  if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return false;
+  }
+  cudaGraph_t g = nullptr;
+  try {
+    pcg_iteration_body(c, n, flexible);
+  } catch (...) {
+    cudaStreamEndCapture(s, &g);
+    if (g) cudaGraphDestroy(g);
+    (void)cudaGetLastError();
+    g_kernel_launches.store(before);
+    return false;
+  }
+  if (cudaStreamEndCapture(s, &g) != cudaSuccess || !g) {
+    (void)cudaGetLastError();
+    g_kernel_launches.store(before);
+    return false;
+  }
+  cudaError_t e = cudaGraphInstantiate(&c.pcg_exec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    c.pcg_exec = nullptr;
+    g_kernel_launches.store(before);
+    return false;
+  }
+  c.graph_nodes = g_kernel_launches.load() - before;
+  g_kernel_launches.store(before);  // counted per replay below
+  c.graph_gen = c.hier_gen;
+  c.graph_flexible = flexible;
+  return true;
+}
+
+template <class T>
+void set_all_smem_attrs(Hierarchy<T>& H) {
+  for (auto& L : H.L)
+    if (!L->coarsest) set_smem_attrs(*L);
+}
+
+}  // namespace
+
 SolveResult amg_solve_device(Ctx& c, const double* d_b, double* d_x) {
   FG_REQUIRE(c.has_hierarchy, FEMGPU_ERR_NOT_READY, "call femgpu_setup first");
   const int n = c.A.n;
   cudaStream_t s = c.stream;
   ensure_work(c, n);
+  if (c.cfg.precision == 1) set_all_smem_attrs(static_cast<Hierarchy<double>&>(*c.H));
+  else set_all_smem_attrs(static_cast<Hierarchy<float>&>(*c.H));
   SolveResult res;
   double* part = c.red.p;
-  double* part2 = c.red.p + kRedBlocks;
   double* sc = c.red.p + 2 * kRedBlocks;
   const DCsr<double>& A = c.A0p;
   FG_LAUNCH(perm_vec_in_kernel, grid_for(n, 256), 256, 0, s, n, c.perm0.p, d_b, c.vb.p);
@@ -452,7 +539,9 @@ SolveResult amg_solve_device(Ctx& c, const double* d_b, double* d_x) {
   FG_LAUNCH(spmv_kernel, grid_for(n, 256), 256, 0, s, n, A.rp.p, A.ci.p, A.v.p, c.vx.p, c.vy.p);
   FG_LAUNCH(residual_kernel, kRedBlocks, kRedThreads, 0, s, n, c.vb.p, c.vy.p, c.vr.p, part);
   FG_LAUNCH(finalize_kernel, 1, 1024, 0, s, part, kRedBlocks, sc + S_NR);
-  FG_CUDA(cudaMemsetAsync(sc + S_FLAG, 0, sizeof(double), s));
+  FG_LAUNCH(set_slot_kernel, 1, 1, 0, s, sc, S_FLAG, 0.0);
+  FG_LAUNCH(set_slot_kernel, 1, 1, 0, s, sc, S_FIRST, 1.0);
+  FG_CUDA(cudaMemsetAsync(c.vp.p, 0, n * sizeof(double), s));
   FG_CUDA(cudaMemcpyAsync(c.h_scalars, sc, S_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s));
   FG_CUDA(cudaStreamSynchronize(s));
   double bnorm = sqrt(c.h_scalars[S_BN]);
@@ -464,18 +553,14 @@ SolveResult amg_solve_device(Ctx& c, const double* d_b, double* d_x) {
   if (nr / bnorm <= tol) {
     res.status = FEMGPU_OK;
   } else {
-    precondition_any(c, c.vr.p, c.vz.p);
-    FG_LAUNCH(copy_kernel, kRedBlocks, kRedThreads, 0, s, n, c.vz.p, c.vp.p);
-    FG_LAUNCH(dot_kernel, kRedBlocks, kRedThreads, 0, s, n, c.vr.p, c.vz.p, nullptr, part, nullptr);
-    FG_LAUNCH(finalize_kernel, 1, 1024, 0, s, part, kRedBlocks, sc + S_RZ);
+    const bool graph = capture_iteration(c, n, flexible);
     while (it < c.cfg.maxIters) {
-      FG_LAUNCH(spmv_dot_kernel, kRedBlocks, kRedThreads, 0, s, n, A.rp.p, A.ci.p, A.v.p, c.vp.p, c.vy.p, part);
-      FG_LAUNCH(finalize_kernel, 1, 1024, 0, s, part, kRedBlocks, sc + S_YP);
-      FG_LAUNCH(alpha_kernel, 1, 1, 0, s, sc);
-      FG_LAUNCH(update_kernel, kRedBlocks, kRedThreads, 0, s, n, sc, c.vp.p, c.vy.p, c.vx.p, c.vr.p,
-                flexible ? c.vrold.p : nullptr, part);
-      FG_LAUNCH(finalize_kernel, 1, 1024, 0, s, part, kRedBlocks, sc + S_NR);
-      FG_CUDA(cudaMemcpyAsync(c.h_scalars, sc, S_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s));
+      if (graph) {
+        FG_CUDA(cudaGraphLaunch(c.pcg_exec, s));
+        g_kernel_launches.fetch_add(c.graph_nodes);
+      } else {
+        pcg_iteration_body(c, n, flexible);
+      }
       FG_CUDA(cudaStreamSynchronize(s));
       it++;
       nr = sqrt(c.h_scalars[S_NR]);
@@ -487,13 +572,6 @@ SolveResult amg_solve_device(Ctx& c, const double* d_b, double* d_x) {
         res.status = FEMGPU_OK;
         break;
       }
-      precondition_any(c, c.vr.p, c.vz.p);
-      FG_LAUNCH(dot_kernel, kRedBlocks, kRedThreads, 0, s, n, c.vz.p, c.vr.p, flexible ? c.vrold.p : nullptr, part,
-                part2);
-      FG_LAUNCH(finalize_kernel, 1, 1024, 0, s, part, kRedBlocks, sc + S_RZNEW);
-      if (flexible) FG_LAUNCH(finalize_kernel, 1, 1024, 0, s, part2, kRedBlocks, sc + S_ZROLD);
-      FG_LAUNCH(beta_kernel, 1, 1, 0, s, sc, flexible);
-      FG_LAUNCH(pupdate_kernel, kRedBlocks, kRedThreads, 0, s, n, sc, c.vz.p, c.vp.p);
     }
   }
   FG_LAUNCH(perm_vec_out_kernel, grid_for(n, 256), 256, 0, s, n, c.perm0.p, c.vx.p, d_x);

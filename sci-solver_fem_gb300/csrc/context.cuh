@@ -92,6 +92,15 @@ struct Ctx {
   DBuf<double> vb, vx, vr, vz, vp, vy, vrold;
   DBuf<double> red;              // reduction partials + scalars
   double* h_scalars = nullptr;   // pinned host mirror of the device scalars
+  // one PCG iteration captured as a CUDA graph, rebuilt when the hierarchy changes
+  uint64_t hier_gen = 0, graph_gen = ~0ull;
+  int graph_flexible = -1;
+  cudaGraphExec_t pcg_exec = nullptr;
+  int64_t graph_nodes = 0;
+
+  ~Ctx() {
+    if (pcg_exec) cudaGraphExecDestroy(pcg_exec);
+  }
 };
 
 // fem_assembly.cu

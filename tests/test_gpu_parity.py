@@ -97,6 +97,20 @@ def test_hierarchy_matches_oracle(precision):
             assert np.array_equal(go["P_vals"], oo["P_vals"]), (l, np.abs(go["P_vals"] - oo["P_vals"]).max())
 
 
+def test_large_hierarchy_with_long_rap_rows():
+    # 96^3 (912,673 DOF): level 2's Galerkin rows exceed the 8192-product shared-memory
+    # sort and take the dense-accumulator path; values must still match bit for bit.
+    orc, s, _ = build_both(n=96, seed=1, precision=0, sigma=2.0)
+    assert s.num_levels == orc.num_levels >= 4
+    for l in range(orc.num_levels):
+        go, oo = s.level(l), orc.level(l)
+        assert go["nnz"] == oo["nnz"] and go["n_agg"] == oo["n_agg"]
+        if oo["n_agg"]:
+            assert np.array_equal(go["perm"], oo["perm"]) and np.array_equal(go["agg_idx"], oo["agg_idx"])
+        if l > 0:
+            assert np.array_equal(go["A_cols"], oo["A_cols"]) and np.array_equal(go["A_vals"], oo["A_vals"])
+
+
 @pytest.mark.parametrize("seed", [1, 2, 99])
 def test_aggregates_bit_exact_across_seeds(seed):
     orc, s, _ = build_both(n=12, seed=seed)
