@@ -1228,13 +1228,33 @@ void post_smooth(Level<T>& L, const orc_config& c) {
   }
 }
 
+/* Row products of the transfer operators in the device's lane order: S lanes per row
+ * (S from the average row length), lane j sums entries j, j+S, ... in order, then
+ * an xor butterfly (p_j + p_{j^off}, off = S/2 .. 1) combines them; lane 0's value is
+ * the result.  The reference's CUSP SpMV order is unpinned. */
+int lanes_for_rows(int64_t nnz, int n) {
+  double avg = n > 0 ? (double)nnz / n : 0.0;
+  int s = 1;
+  while (s < 32 && s * 4 < avg) s <<= 1;
+  return s;
+}
+
 template <class T>
 void spmv_rows(const Csr<T>& A, const std::vector<T>& x, std::vector<T>& y) {
+  const int S = lanes_for_rows(A.nnz(), A.n);
 #pragma omp parallel for schedule(static)
   for (int i = 0; i < A.n; i++) {
-    T s = 0;
-    for (int e = A.rp[i]; e < A.rp[i + 1]; e++) s = s + A.v[e] * x[A.ci[e]];
-    y[i] = s;
+    T p[32], q[32];
+    for (int j = 0; j < S; j++) p[j] = 0;
+    for (int e = A.rp[i]; e < A.rp[i + 1]; e++) {
+      int j = (e - A.rp[i]) % S;
+      p[j] = p[j] + A.v[e] * x[A.ci[e]];
+    }
+    for (int off = S >> 1; off > 0; off >>= 1) {
+      for (int j = 0; j < S; j++) q[j] = p[j] + p[j ^ off];
+      for (int j = 0; j < S; j++) p[j] = q[j];
+    }
+    y[i] = p[0];
   }
 }
 

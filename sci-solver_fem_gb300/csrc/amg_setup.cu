@@ -13,6 +13,8 @@
 // results use fixed summation orders (see row_esc_kernel).
 #include <algorithm>
 #include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <cmath>
 
 #include "context.cuh"
@@ -556,7 +558,7 @@ struct EscArgs {
   int32_t* overflow;
 };
 
-constexpr int kEscWarpCap = 512;
+constexpr int kEscWarpCap = 1024;
 constexpr int kEscWarps = 4;
 constexpr int kEscBlockCap = 8192;
 constexpr int kEscBlockThreads = 512;
@@ -646,43 +648,44 @@ __device__ void esc_generate(const EscArgs<T>& a, int i, unsigned long long* key
   }
 }
 
-// After sorting: count (pass 1) or write (pass 2) the reduced row.
+// After sorting: count (pass 1) or write (pass 2) the reduced row.  Heads are the
+// first item of each column run; each head's thread sums its run left to right.
+// Heads are ranked by warp ballots plus an exclusive scan over the warps.
 template <class T, class Sync>
-__device__ int esc_reduce(const unsigned long long* keys, const T* vals_by_gen, int len, int tid, int nthr, int* s_cnt,
-                          int32_t* oci, T* ov, bool write, Sync sync) {
-  // heads: positions whose column differs from the previous one
-  if (tid == 0) *s_cnt = 0;
-  sync();
-  // count heads per thread-chunk sequentially in a fixed chunk order
+__device__ int esc_reduce(const unsigned long long* keys, const T* vals_by_gen, int len, int tid, int nthr,
+                          int* s_warp /* >= nthr/32 + 1 ints */, int32_t* oci, T* ov, bool write, Sync sync) {
+  const int lane = tid & 31, w = tid >> 5, nw = (nthr + 31) >> 5;
   int total = 0;
   for (int c0 = 0; c0 < len; c0 += nthr) {
-    int p = c0 + tid;
-    bool head = p < len && (p == 0 || (keys[p] >> 32) != (keys[p - 1] >> 32));
-    // rank among heads within this chunk
-    __shared__ int s_flags[kEscBlockThreads];
-    int* flags = s_flags + ((nthr == 32) ? (threadIdx.x & ~31) : 0);
-    flags[tid] = head ? 1 : 0;
-    sync();
-    int rank = 0, chunk_heads = 0;
-    if (nthr == 32) {
-      unsigned m = __ballot_sync(0xffffffffu, head);
-      rank = __popc(m & ((1u << tid) - 1u));
-      chunk_heads = __popc(m);
-    } else {
-      for (int t = 0; t < nthr; t++) {
-        if (t < tid) rank += flags[t];
-        chunk_heads += flags[t];
+    const int p = c0 + tid;
+    const bool head = p < len && (p == 0 || (keys[p] >> 32) != (keys[p - 1] >> 32));
+    const unsigned m = __ballot_sync(0xffffffffu, head);
+    int rank = __popc(m & ((1u << lane) - 1u)), chunk = __popc(m);
+    if (nw > 1) {
+      if (lane == 0) s_warp[w] = chunk;
+      sync();
+      if (tid == 0) {
+        int t = 0;
+        for (int k = 0; k < nw; k++) {
+          int v = s_warp[k];
+          s_warp[k] = t;
+          t += v;
+        }
+        s_warp[nw] = t;
       }
+      sync();
+      rank += s_warp[w];
+      chunk = s_warp[nw];
     }
     if (head && write) {
-      unsigned col = (unsigned)(keys[p] >> 32);
+      const unsigned col = (unsigned)(keys[p] >> 32);
       T sum = vals_by_gen[(unsigned)(keys[p] & 0xffffffffu)];
       for (int q = p + 1; q < len && (unsigned)(keys[q] >> 32) == col; q++)
         sum = sum + vals_by_gen[(unsigned)(keys[q] & 0xffffffffu)];
       oci[total + rank] = (int32_t)col;
       ov[total + rank] = sum;
     }
-    total += chunk_heads;
+    total += chunk;
     sync();
   }
   return total;
@@ -731,7 +734,7 @@ __global__ void esc_block_kernel(EscArgs<T> a, const int32_t* items) {
   unsigned long long* keys = reinterpret_cast<unsigned long long*>(smem_raw);
   T* vals = reinterpret_cast<T*>(keys + kEscBlockCap);
   __shared__ int s_scan[kEscBlockThreads];
-  __shared__ int s_cnt;
+  __shared__ int s_cnt[kEscBlockThreads / 32 + 1];
   for (int b = blockIdx.x; b < a.nbig; b += gridDim.x) {
     int i = a.big_rows[b];
     int len = items[i];
@@ -741,7 +744,7 @@ __global__ void esc_block_kernel(EscArgs<T> a, const int32_t* items) {
     __syncthreads();
     bitonic_sort_shared(keys, np2, threadIdx.x, blockDim.x, BlockSync());
     int out = WRITE ? a.orp[i] : 0;
-    int cnt = esc_reduce<T>(keys, vals, len, threadIdx.x, blockDim.x, &s_cnt, WRITE ? a.oci + out : nullptr,
+    int cnt = esc_reduce<T>(keys, vals, len, threadIdx.x, blockDim.x, s_cnt, WRITE ? a.oci + out : nullptr,
                             WRITE ? a.ov + out : nullptr, WRITE, BlockSync());
     if (!WRITE && threadIdx.x == 0) a.counts[i] = cnt;
     __syncthreads();
@@ -1075,6 +1078,36 @@ __global__ void partition_rows_kernel(int npart, const int32_t* part_idx, const 
   if (p < npart) rows[p] = agg_idx[part_idx[p + 1]] - agg_idx[part_idx[p]];
 }
 
+// In-partition entries per partition (the shared-memory footprint of the smoother).
+__global__ void partition_entries_kernel(int npart, const int32_t* part_idx, const int32_t* agg_idx,
+                                         const int32_t* irp, int32_t* ent) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < npart) ent[p] = irp[agg_idx[part_idx[p + 1]]] - irp[agg_idx[part_idx[p]]];
+}
+
+// Opt-in setup phase timing (environment FEMGPU_PROFILE set): synchronizes between
+// phases and prints the host wall time of each to stderr.
+struct PhaseTimer {
+  bool on;
+  cudaStream_t s;
+  int level;
+  std::chrono::steady_clock::time_point t0;
+  PhaseTimer(cudaStream_t st, int lvl) : on(getenv("FEMGPU_PROFILE") != nullptr), s(st), level(lvl) {
+    if (on) {
+      cudaStreamSynchronize(s);
+      t0 = std::chrono::steady_clock::now();
+    }
+  }
+  void mark(const char* what) {
+    if (!on) return;
+    cudaStreamSynchronize(s);
+    auto t = std::chrono::steady_clock::now();
+    fprintf(stderr, "[femgpu setup] level %d %-10s %8.3f ms\n", level, what,
+            std::chrono::duration<double, std::milli>(t - t0).count());
+    t0 = t;
+  }
+};
+
 template <class T>
 void build_levels(Ctx& c, Hierarchy<T>& H) {
   cudaStream_t s = c.stream;
@@ -1119,8 +1152,10 @@ void build_levels(Ctx& c, Hierarchy<T>& H) {
       L.x.alloc(N, s);
       break;
     }
+    PhaseTimer pt(s, num_levels - 1);
     OldMisOut o;
     old_mis(c, N, L.gxadj.p, L.gadj.p, o);
+    pt.mark("aggregate");
     L.nagg = o.nagg;
     L.npart = o.npart;
     L.perm = std::move(o.perm);
@@ -1138,6 +1173,7 @@ void build_levels(Ctx& c, Hierarchy<T>& H) {
       a.iperm = L.iperm.p;
       run_esc<T, ESC_PERMUTE>(c, a, N, N, L.Ap);
     }
+    pt.mark("permute");
     L.diag.alloc(N, s);
     FG_LAUNCH(diag_kernel<T>, grid_for(N, 256), 256, 0, s, N, L.Ap.rp.p, L.Ap.ci.p, L.Ap.v.p, L.diag.p);
     // in/out-of-partition split
@@ -1158,10 +1194,14 @@ void build_levels(Ctx& c, Hierarchy<T>& H) {
                 o.part_of_row.p, L.Ain.rp.p, L.Ain.ci.p, L.Ain.v.p, L.Aout.rp.p, L.Aout.ci.p, L.Aout.v.p);
     }
     {
-      DBuf<int32_t> prow(L.npart + 1, s);
+      DBuf<int32_t> prow(L.npart + 1, s), pent(L.npart + 1, s);
       FG_LAUNCH(partition_rows_kernel, grid_for(L.npart, 256), 256, 0, s, L.npart, L.part_idx.p, L.agg_idx.p, prow.p);
       L.max_part_rows = reduce_max(prow.p, L.npart, s);
+      FG_LAUNCH(partition_entries_kernel, grid_for(L.npart, 256), 256, 0, s, L.npart, L.part_idx.p, L.agg_idx.p,
+                L.Ain.rp.p, pent.p);
+      L.max_part_entries = reduce_max(pent.p, L.npart, s);
     }
+    pt.mark("split");
     // prolongator and restrictor
     {
       EscArgs<T> a{};
@@ -1174,6 +1214,7 @@ void build_levels(Ctx& c, Hierarchy<T>& H) {
       run_esc<T, ESC_PROLONG>(c, a, N, L.nagg, L.P);
     }
     {
+      pt.mark("P");
       DCsr<T> Ru;  // unsorted transpose, then rows sorted by column
       Ru.n = L.nagg;
       Ru.m = N;
@@ -1205,7 +1246,9 @@ void build_levels(Ctx& c, Hierarchy<T>& H) {
       a.brp = L.P.rp.p;
       a.bci = L.P.ci.p;
       a.bv = L.P.v.p;
+      pt.mark("R");
       run_esc<T, ESC_SPGEMM>(c, a, N, L.nagg, AP);
+      pt.mark("AP");
       EscArgs<T> r{};
       r.arp = L.R.rp.p;
       r.aci = L.R.ci.p;
@@ -1214,6 +1257,7 @@ void build_levels(Ctx& c, Hierarchy<T>& H) {
       r.bci = AP.ci.p;
       r.bv = AP.v.p;
       run_esc<T, ESC_SPGEMM>(c, r, L.nagg, L.nagg, nx->A);
+      pt.mark("RAP");
     }
     nx->n = L.nagg;
     nx->gxadj = std::move(o.xadj_out);

@@ -85,38 +85,103 @@ __device__ __forceinline__ T in_row_sum(const int32_t* __restrict__ rp, const in
   return s;
 }
 
-// Pre-smoother of one partition: x0 = w b / d, nInner Jacobi sweeps, in-partition residual.
+// Shared-memory layout of one partition in the smoother: x, the in-partition sums,
+// the right-hand side, the diagonal, local row offsets and (when it fits) the
+// partition's block of in-partition entries with 16-bit local column indices.
 template <class T>
-__global__ void pre_smooth_kernel(const int32_t* __restrict__ part_idx, const int32_t* __restrict__ agg_idx,
-                                  const int32_t* __restrict__ irp, const int32_t* __restrict__ ici,
-                                  const T* __restrict__ iv, const T* __restrict__ diag, const T* __restrict__ b,
-                                  double w, int inner, T* __restrict__ x, T* __restrict__ r) {
-  extern __shared__ unsigned char sm[];
+struct PartSmem {
+  T *sx, *sax, *sb, *sd, *sval;
+  int32_t* srp;
+  uint16_t* scol;
+};
+
+template <class T>
+__device__ __forceinline__ PartSmem<T> carve(unsigned char* sm, int mcap, int ecap) {
+  PartSmem<T> L;
+  L.sx = reinterpret_cast<T*>(sm);
+  L.sax = L.sx + mcap;
+  L.sb = L.sax + mcap;
+  L.sd = L.sb + mcap;
+  L.sval = L.sd + mcap;
+  L.srp = reinterpret_cast<int32_t*>(L.sval + ecap);
+  L.scol = reinterpret_cast<uint16_t*>(L.srp + mcap + 1);
+  return L;
+}
+
+template <class T>
+size_t part_smem_bytes(int mcap, int ecap) {
+  return (size_t)mcap * 4 * sizeof(T) + (size_t)ecap * sizeof(T) + (size_t)(mcap + 1) * 4 + (size_t)ecap * 2 + 16;
+}
+
+// Sum over row t's in-partition entries in ascending column order, products rounded
+// separately (the reference adds them with shared-memory atomics in any order).
+template <class T, bool STAGED>
+__device__ __forceinline__ T part_row_sum(const PartSmem<T>& P, int t, const int32_t* __restrict__ ici,
+                                          const T* __restrict__ iv, int es, int rs) {
+  T s = 0;
+  const int q0 = P.srp[t], q1 = P.srp[t + 1];
+  for (int q = q0; q < q1; q++) {
+    if (STAGED) s = s + P.sval[q] * P.sx[P.scol[q]];
+    else s = s + iv[es + q] * P.sx[ici[es + q] - rs];
+  }
+  return s;
+}
+
+// Partition-block Jacobi smoother, one CTA per partition.
+// POST == false (preRRSym_kernel + the in-partition part of the residual,
+//   gauss_seidel.cu:1278-1376): x0 = w b / d, `inner` sweeps, then x and
+//   r = b - A_in x - d x are written;
+// POST == true (postRelaxSym_kernel, gauss_seidel.cu:3626-3736): b' = b - A_out x_in,
+//   `inner` sweeps from x_in, result written to x_out.
+template <class T, bool POST, bool STAGED>
+__global__ void __launch_bounds__(256) smooth_kernel(
+    const int32_t* __restrict__ part_idx, const int32_t* __restrict__ agg_idx, const int32_t* __restrict__ irp,
+    const int32_t* __restrict__ ici, const T* __restrict__ iv, const int32_t* __restrict__ orp,
+    const int32_t* __restrict__ oci, const T* __restrict__ ov, const T* __restrict__ diag, const T* __restrict__ b,
+    double w, int inner, const T* __restrict__ x_in, T* __restrict__ x_out, T* __restrict__ r_out, int mcap,
+    int ecap) {
+  extern __shared__ __align__(16) unsigned char sm[];
   const int rs = agg_idx[part_idx[blockIdx.x]], re = agg_idx[part_idx[blockIdx.x + 1]];
   const int m = re - rs;
-  T* sx = reinterpret_cast<T*>(sm);
-  T* sax = sx + m;
+  const int es = irp[rs], ne = irp[re] - es;
+  PartSmem<T> P = carve<T>(sm, mcap, STAGED ? ecap : 0);
   for (int t = threadIdx.x; t < m; t += blockDim.x) {
-    int row = rs + t;
-    sx[t] = (T)((w * (double)b[row]) / (double)diag[row]);
+    const int row = rs + t;
+    const T d = diag[row];
+    P.sd[t] = d;
+    P.srp[t] = irp[row] - es;
+    if (POST) {
+      T acc = b[row];
+      for (int e = orp[row]; e < orp[row + 1]; e++) acc = acc + (-ov[e]) * x_in[oci[e]];
+      P.sb[t] = acc;
+      P.sx[t] = x_in[row];
+    } else {
+      const T bv = b[row];
+      P.sb[t] = bv;
+      P.sx[t] = (T)((w * (double)bv) / (double)d);
+    }
   }
+  if (threadIdx.x == 0) P.srp[m] = ne;
+  if (STAGED)
+    for (int q = threadIdx.x; q < ne; q += blockDim.x) {
+      P.sval[q] = iv[es + q];
+      P.scol[q] = (uint16_t)(ici[es + q] - rs);
+    }
   __syncthreads();
   for (int it = 0; it < inner; it++) {
-    for (int t = threadIdx.x; t < m; t += blockDim.x) sax[t] = in_row_sum(irp, ici, iv, rs + t, rs, sx);
+    for (int t = threadIdx.x; t < m; t += blockDim.x) P.sax[t] = part_row_sum<T, STAGED>(P, t, ici, iv, es, rs);
     __syncthreads();
-    for (int t = threadIdx.x; t < m; t += blockDim.x) {
-      int row = rs + t;
-      sx[t] = relax(sx[t], b[row], sax[t], diag[row], w);
-    }
+    for (int t = threadIdx.x; t < m; t += blockDim.x) P.sx[t] = relax(P.sx[t], P.sb[t], P.sax[t], P.sd[t], w);
     __syncthreads();
   }
   for (int t = threadIdx.x; t < m; t += blockDim.x) {
-    int row = rs + t;
-    T s = in_row_sum(irp, ici, iv, row, rs, sx);
-    T xv = sx[t];
-    x[row] = xv;
-    T u = b[row] - s;
-    r[row] = u - diag[row] * xv;
+    const int row = rs + t;
+    const T xv = P.sx[t];
+    x_out[row] = xv;
+    if (!POST) {
+      T u = P.sb[t] - part_row_sum<T, STAGED>(P, t, ici, iv, es, rs);
+      r_out[row] = u - P.sd[t] * xv;
+    }
   }
 }
 
@@ -131,47 +196,21 @@ __global__ void aout_residual_kernel(int n, const int32_t* __restrict__ orp, con
   r[i] = r[i] - s;
 }
 
-// y = M x (accumulate = 0) or y = y + M x (accumulate = 1), rows summed in order.
-template <class T>
-__global__ void spmv_seq_kernel(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
-                                const T* __restrict__ v, const T* __restrict__ x, T* __restrict__ y, int accumulate) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+// y = M x (accumulate = 0) or y = y + M x (accumulate = 1) with S lanes per row:
+// lane j sums entries j, j+S, ... in order, then an xor butterfly combines the lanes.
+// S comes from lanes_for_rows(); the CPU oracle evaluates the same order.
+template <class T, int S>
+__global__ void spmv_lanes_kernel(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                  const T* __restrict__ v, const T* __restrict__ x, T* __restrict__ y, int accumulate) {
+  const int g = (blockIdx.x * blockDim.x + threadIdx.x) / S;
+  const int j = threadIdx.x & (S - 1);
+  const bool live = g < n;
   T s = 0;
-  for (int e = rp[i]; e < rp[i + 1]; e++) s = s + v[e] * x[ci[e]];
-  y[i] = accumulate ? y[i] + s : s;
-}
-
-// Post-smoother relax of one partition (postRelaxSym_kernel): b' = b - A_out x, then
-// nInner Jacobi sweeps from the current x; result to xo.
-template <class T>
-__global__ void post_smooth_kernel(const int32_t* __restrict__ part_idx, const int32_t* __restrict__ agg_idx,
-                                   const int32_t* __restrict__ irp, const int32_t* __restrict__ ici,
-                                   const T* __restrict__ iv, const int32_t* __restrict__ orp,
-                                   const int32_t* __restrict__ oci, const T* __restrict__ ov,
-                                   const T* __restrict__ diag, const T* __restrict__ b, double w, int inner,
-                                   const T* __restrict__ x, T* __restrict__ xo) {
-  extern __shared__ unsigned char sm[];
-  const int rs = agg_idx[part_idx[blockIdx.x]], re = agg_idx[part_idx[blockIdx.x + 1]];
-  const int m = re - rs;
-  T* sx = reinterpret_cast<T*>(sm);
-  T* sax = sx + m;
-  T* sb = sax + m;
-  for (int t = threadIdx.x; t < m; t += blockDim.x) {
-    int row = rs + t;
-    T s = b[row];
-    for (int e = orp[row]; e < orp[row + 1]; e++) s = s + (-ov[e]) * x[oci[e]];
-    sb[t] = s;
-    sx[t] = x[row];
-  }
-  __syncthreads();
-  for (int it = 0; it < inner; it++) {
-    for (int t = threadIdx.x; t < m; t += blockDim.x) sax[t] = in_row_sum(irp, ici, iv, rs + t, rs, sx);
-    __syncthreads();
-    for (int t = threadIdx.x; t < m; t += blockDim.x) sx[t] = relax(sx[t], sb[t], sax[t], diag[rs + t], w);
-    __syncthreads();
-  }
-  for (int t = threadIdx.x; t < m; t += blockDim.x) xo[rs + t] = sx[t];
+  if (live)
+    for (int e = rp[g] + j; e < rp[g + 1]; e += S) s = s + v[e] * x[ci[e]];
+#pragma unroll
+  for (int off = S >> 1; off > 0; off >>= 1) s = s + __shfl_xor_sync(0xffffffffu, s, off, S);
+  if (live && j == 0) y[g] = accumulate ? y[g] + s : s;
 }
 
 // Coarsest level: x = A^-1 b with the explicit FP64 inverse.
@@ -296,10 +335,6 @@ __global__ void pupdate_kernel(int n, const double* __restrict__ sc, const doubl
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = fma(beta, p[i], z[i]);
 }
 
-__global__ void copy_kernel(int n, const double* __restrict__ a, double* __restrict__ b) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = a[i];
-}
-
 __global__ void perm_vec_in_kernel(int n, const int32_t* perm, const double* in, double* out) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[perm[i]] = in[i];
@@ -311,24 +346,64 @@ __global__ void perm_vec_out_kernel(int n, const int32_t* perm, const double* in
 }
 
 // ---- V-cycle driver ------------------------------------------------------------------
-template <class T>
-size_t pre_smem(const Level<T>& L) {
-  return (size_t)2 * L.max_part_rows * sizeof(T);
+constexpr size_t kStageLimit = 160 * 1024;  // staged smoother: keep >= 1 CTA per SM with room
+
+// Lanes per row for the R/P products: the same rule in the CPU oracle.
+inline int lanes_for_rows(int64_t nnz, int n) {
+  double avg = n > 0 ? (double)nnz / n : 0.0;
+  int s = 1;
+  while (s < 32 && s * 4 < avg) s <<= 1;
+  return s;
 }
 
 template <class T>
-int smooth_threads(const Level<T>& L) {
-  int t = ((L.max_part_rows + 31) / 32) * 32;
-  return t < 32 ? 32 : (t > 1024 ? 1024 : t);
+void spmv_lanes(const DCsr<T>& M, const T* x, T* y, int accumulate, cudaStream_t st) {
+  const int S = lanes_for_rows(M.nnz, M.n);
+  const int64_t threads = (int64_t)M.n * S;
+  const int g = grid_for(threads, 256);
+  switch (S) {
+    case 1: FG_LAUNCH((spmv_lanes_kernel<T, 1>), g, 256, 0, st, M.n, M.rp.p, M.ci.p, M.v.p, x, y, accumulate); break;
+    case 2: FG_LAUNCH((spmv_lanes_kernel<T, 2>), g, 256, 0, st, M.n, M.rp.p, M.ci.p, M.v.p, x, y, accumulate); break;
+    case 4: FG_LAUNCH((spmv_lanes_kernel<T, 4>), g, 256, 0, st, M.n, M.rp.p, M.ci.p, M.v.p, x, y, accumulate); break;
+    case 8: FG_LAUNCH((spmv_lanes_kernel<T, 8>), g, 256, 0, st, M.n, M.rp.p, M.ci.p, M.v.p, x, y, accumulate); break;
+    case 16: FG_LAUNCH((spmv_lanes_kernel<T, 16>), g, 256, 0, st, M.n, M.rp.p, M.ci.p, M.v.p, x, y, accumulate); break;
+    default: FG_LAUNCH((spmv_lanes_kernel<T, 32>), g, 256, 0, st, M.n, M.rp.p, M.ci.p, M.v.p, x, y, accumulate); break;
+  }
+}
+
+template <class T>
+bool staged(const Level<T>& L) {
+  return L.max_part_rows < 65536 && part_smem_bytes<T>(L.max_part_rows, L.max_part_entries) <= kStageLimit;
+}
+
+template <class T>
+size_t smooth_smem(const Level<T>& L) {
+  return part_smem_bytes<T>(L.max_part_rows, staged(L) ? L.max_part_entries : 0);
 }
 
 template <class T>
 void set_smem_attrs(const Level<T>& L) {
-  size_t post = (size_t)3 * L.max_part_rows * sizeof(T);
-  if (post > 48 * 1024) {
-    FG_CUDA(cudaFuncSetAttribute(pre_smooth_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)post));
-    FG_CUDA(cudaFuncSetAttribute(post_smooth_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)post));
-  }
+  const int bytes = (int)smooth_smem(L);
+  if (bytes <= 48 * 1024) return;
+  FG_CUDA(cudaFuncSetAttribute(smooth_kernel<T, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  FG_CUDA(cudaFuncSetAttribute(smooth_kernel<T, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  FG_CUDA(cudaFuncSetAttribute(smooth_kernel<T, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  FG_CUDA(cudaFuncSetAttribute(smooth_kernel<T, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+}
+
+template <class T>
+void smooth(Ctx& c, Level<T>& L, bool post, const T* b, const T* xin, T* xout, T* rout) {
+  cudaStream_t s = c.stream;
+  const double w = c.cfg.smootherWeight;
+  const int inner = post ? c.cfg.postInnerIters : c.cfg.preInnerIters;
+  const size_t sm = smooth_smem(L);
+  const bool st = staged(L);
+  auto k = post ? (st ? smooth_kernel<T, true, true> : smooth_kernel<T, true, false>)
+                : (st ? smooth_kernel<T, false, true> : smooth_kernel<T, false, false>);
+  // the limit is a per-function attribute shared by every handle: set it per launch
+  if (sm > 48 * 1024) FG_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  FG_LAUNCH(k, L.npart, 256, sm, s, L.part_idx.p, L.agg_idx.p, L.Ain.rp.p, L.Ain.ci.p, L.Ain.v.p, L.Aout.rp.p,
+            L.Aout.ci.p, L.Aout.v.p, L.diag.p, b, w, inner, xin, xout, rout, L.max_part_rows, L.max_part_entries);
 }
 
 // b (level order for l > 0, already permuted for l == 0) -> x (same ordering).
@@ -341,29 +416,23 @@ void vcycle(Ctx& c, Hierarchy<T>& H, int l, const T* b_in, T* x_out) {
     FG_LAUNCH(coarse_solve_kernel<T>, grid_for(n, 128), 128, 0, s, n, L.Ainv.p, b_in, x_out);
     return;
   }
-  const double w = c.cfg.smootherWeight;
   const T* b = b_in;
   if (l > 0) {
     FG_LAUNCH(permute_in_kernel<T>, grid_for(n, 256), 256, 0, s, n, L.iperm.p, b_in, L.b.p);
     b = L.b.p;
   }
-  set_smem_attrs(L);
-  const int thr = smooth_threads(L);
-  FG_LAUNCH(pre_smooth_kernel<T>, L.npart, thr, pre_smem(L), s, L.part_idx.p, L.agg_idx.p, L.Ain.rp.p, L.Ain.ci.p,
-            L.Ain.v.p, L.diag.p, b, w, c.cfg.preInnerIters, L.x.p, L.r.p);
+  smooth<T>(c, L, false, b, nullptr, L.x.p, L.r.p);
   FG_LAUNCH(aout_residual_kernel<T>, grid_for(n, 256), 256, 0, s, n, L.Aout.rp.p, L.Aout.ci.p, L.Aout.v.p, L.x.p,
             L.r.p);
   // next level: input in its t (or b when coarsest), output in its xo (or x)
   Level<T>& N = *H.L[l + 1];
   T* bc = N.coarsest ? N.b.p : N.t.p;
   T* xc = N.coarsest ? N.x.p : N.xo.p;
-  FG_LAUNCH(spmv_seq_kernel<T>, grid_for(L.nagg, 128), 128, 0, s, L.nagg, L.R.rp.p, L.R.ci.p, L.R.v.p, L.r.p, bc, 0);
+  spmv_lanes(L.R, L.r.p, bc, 0, s);
   vcycle(c, H, l + 1, bc, xc);
-  FG_LAUNCH(spmv_seq_kernel<T>, grid_for(n, 128), 128, 0, s, n, L.P.rp.p, L.P.ci.p, L.P.v.p, xc, L.x.p, 1);
+  spmv_lanes(L.P, xc, L.x.p, 1, s);
   for (int rl = 0; rl < c.cfg.postRelaxes; rl++) {
-    FG_LAUNCH(post_smooth_kernel<T>, L.npart, thr, (size_t)3 * L.max_part_rows * sizeof(T), s, L.part_idx.p,
-              L.agg_idx.p, L.Ain.rp.p, L.Ain.ci.p, L.Ain.v.p, L.Aout.rp.p, L.Aout.ci.p, L.Aout.v.p, L.diag.p, b, w,
-              c.cfg.postInnerIters, L.x.p, L.r.p);
+    smooth<T>(c, L, true, b, L.x.p, L.r.p, nullptr);
     std::swap(L.x.p, L.r.p);  // r is free after the restriction: use it as the ping-pong buffer
   }
   if (l > 0) {

@@ -51,6 +51,7 @@ struct Level {
   DCsr<T> Ap, Ain, Aout, P, R;
   DBuf<T> diag;
   int max_part_rows = 0;
+  int max_part_entries = 0;  // in-partition off-diagonal entries of the largest partition
   // coarsest: explicit inverse, row-major n x n
   DBuf<double> Ainv;
   // work vectors (level numbering / permuted numbering)
