@@ -809,7 +809,7 @@ struct Level {
   std::vector<int32_t> perm, iperm, aggIdx, partIdx, partLabel, aggOf;
   std::vector<int32_t> gxadj, gadj; /* this level's graph */
   Csr<T> Ap;         /* permuted matrix */
-  std::vector<T> diag;
+  std::vector<T> diag, dinv;
   Csr<T> Ain, Aout;  /* in-partition off-diagonal (upper values mirrored), cross-partition */
   Csr<T> P, R;
   /* coarsest: dense factor */
@@ -1125,6 +1125,8 @@ int setup_levels(orc_amg* h, std::vector<Level<T>>& L, const Csr<double>& A, con
       int64_t d = find_col(lv.Ap.rp.data(), lv.Ap.ci.data(), i, i);
       lv.diag[i] = d >= 0 ? lv.Ap.v[d] : (T)0;
     }
+    lv.dinv.resize(N);
+    for (int i = 0; i < N; i++) lv.dinv[i] = (T)1 / lv.diag[i];
     split_partitions(lv);
     lv.P = build_prolongator(lv.Ap, lv.diag, lv.aggOf, nagg, c.pro_omega);
     lv.R = transpose(lv.P);
@@ -1146,19 +1148,21 @@ int setup_levels(orc_amg* h, std::vector<Level<T>>& L, const Csr<double>& A, con
   return 0;
 }
 
-/* gauss_seidel in-partition sweep update (gauss_seidel.cu:1333-1341): the weight is
- * a double, so the correction is formed in double and rounded back to T. */
+/* gauss_seidel in-partition sweep update x += w (b - sAx - d x) / d
+ * (gauss_seidel.cu:1333-1341), evaluated in T with the precomputed reciprocal of
+ * the diagonal.  (The reference forms it in double because its weight is a double;
+ * the device does the same T arithmetic as here.) */
 template <class T>
-inline T relax_update(T x, T b, T sAx, T d, double w) {
+inline T relax_update(T x, T b, T sAx, T d, T dinv, T w) {
   T t = b - sAx;
   t = t - d * x;
-  return (T)((double)x + (w * (double)t) / (double)d);
+  return x + (w * t) * dinv;
 }
 
 template <class T>
 void pre_smooth(Level<T>& L, const orc_config& c) {
   int np = (int)L.partIdx.size() - 1;
-  const double w = c.smoother_weight;
+  const T w = (T)c.smoother_weight;
 #pragma omp parallel
   {
     std::vector<T> sAx;
@@ -1166,14 +1170,14 @@ void pre_smooth(Level<T>& L, const orc_config& c) {
     for (int p = 0; p < np; p++) {
       int rs = L.aggIdx[L.partIdx[p]], re = L.aggIdx[L.partIdx[p + 1]];
       sAx.assign(re - rs, (T)0);
-      for (int i = rs; i < re; i++) L.x[i] = (T)((w * (double)L.b[i]) / (double)L.diag[i]);
+      for (int i = rs; i < re; i++) L.x[i] = (w * L.b[i]) * L.dinv[i];
       for (int it = 0; it < c.pre_inner; it++) {
         for (int i = rs; i < re; i++) {
           T s = 0;
           for (int e = L.Ain.rp[i]; e < L.Ain.rp[i + 1]; e++) s = s + L.Ain.v[e] * L.x[L.Ain.ci[e]];
           sAx[i - rs] = s;
         }
-        for (int i = rs; i < re; i++) L.x[i] = relax_update(L.x[i], L.b[i], sAx[i - rs], L.diag[i], w);
+        for (int i = rs; i < re; i++) L.x[i] = relax_update(L.x[i], L.b[i], sAx[i - rs], L.diag[i], L.dinv[i], w);
       }
       for (int i = rs; i < re; i++) {
         T s = 0;
@@ -1195,7 +1199,7 @@ void pre_smooth(Level<T>& L, const orc_config& c) {
 template <class T>
 void post_smooth(Level<T>& L, const orc_config& c) {
   int np = (int)L.partIdx.size() - 1;
-  const double w = c.smoother_weight;
+  const T w = (T)c.smoother_weight;
   for (int rl = 0; rl < c.post_relaxes; rl++) {
 #pragma omp parallel
     {
@@ -1219,7 +1223,7 @@ void post_smooth(Level<T>& L, const orc_config& c) {
             for (int e = L.Ain.rp[i]; e < L.Ain.rp[i + 1]; e++) s = s + L.Ain.v[e] * sx[L.Ain.ci[e] - rs];
             sAx[i - rs] = s;
           }
-          for (int i = rs; i < re; i++) sx[i - rs] = relax_update(sx[i - rs], sb[i - rs], sAx[i - rs], L.diag[i], w);
+          for (int i = rs; i < re; i++) sx[i - rs] = relax_update(sx[i - rs], sb[i - rs], sAx[i - rs], L.diag[i], L.dinv[i], w);
         }
         for (int i = rs; i < re; i++) L.xo[i] = sx[i - rs];
       }

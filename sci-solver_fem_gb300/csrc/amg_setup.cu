@@ -556,6 +556,7 @@ struct EscArgs {
   int32_t* oci;
   T* ov;
   int32_t* overflow;
+  int thread_cap;        // rows with at most this many items use the thread tier
 };
 
 constexpr int kEscWarpCap = 1024;
@@ -714,7 +715,7 @@ __global__ void esc_warp_kernel(EscArgs<T> a, const int32_t* items) {
   __shared__ int s_cnt[kEscWarps];
   for (int i = blockIdx.x * kEscWarps + w; i < a.n; i += gridDim.x * kEscWarps) {
     int len = items[i];
-    if (len > kEscWarpCap) continue;
+    if (len > kEscWarpCap || len <= a.thread_cap) continue;
     esc_generate<T, MODE>(a, i, keys, vals, lane, 32, s_scan[w], WarpSync());
     int np2 = next_pow2(len < 2 ? 2 : len);
     for (int p = len + lane; p < np2; p += 32) keys[p] = ~0ull;
@@ -835,8 +836,60 @@ __global__ void collect_dense_rows_kernel(int n, const int32_t* items, int cap, 
   if (i < n && items[i] > cap) list[atomicAdd(nlist, 1)] = i;
 }
 
+// ---- thread tier: short PERMUTE / PROLONG rows, one thread per row -----------------
+// Items are generated in order and merged into a sorted local list; a repeated
+// column adds to its running sum (left to right from the first item).
+constexpr int kThreadRowCap = 32;
+
+template <class T, int MODE, bool WRITE>
+__global__ void esc_thread_kernel(EscArgs<T> a, const int32_t* items) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const int len = items[i];
+  if (len > kThreadRowCap) return;
+  int cols[kThreadRowCap];
+  T vals[kThreadRowCap];
+  int u = 0;
+  auto add = [&](int col, T v) {
+    int p = u;
+    while (p > 0 && cols[p - 1] > col) p--;
+    if (p > 0 && cols[p - 1] == col) {
+      vals[p - 1] = vals[p - 1] + v;
+      return;
+    }
+    for (int q = u; q > p; q--) {
+      cols[q] = cols[q - 1];
+      vals[q] = vals[q - 1];
+    }
+    cols[p] = col;
+    vals[p] = v;
+    u++;
+  };
+  const int r = esc_input_row<T, MODE>(a, i);
+  for (int q = a.arp[r]; q < a.arp[r + 1]; q++) {
+    const int j = a.aci[q];
+    if (MODE == ESC_PERMUTE) {
+      add(a.perm ? a.perm[j] : j, a.av[q]);
+    } else {
+      T t = (a.neg_omega * a.av[q]) * (T)1;
+      add(a.agg_of[j], t / a.diag[i]);
+    }
+  }
+  if (MODE == ESC_PROLONG) add(a.agg_of[i], (T)1);
+  if (WRITE) {
+    const int o = a.orp[i];
+    for (int q = 0; q < u; q++) {
+      a.oci[o + q] = cols[q];
+      a.ov[o + q] = vals[q];
+    }
+  } else {
+    a.counts[i] = u;
+  }
+}
+
+
 template <class T, int MODE>
-void run_esc(Ctx& c, EscArgs<T> a, int nrows_out, int ncols_out, DCsr<T>& out) {
+void run_esc_sort(Ctx& c, EscArgs<T> a, int nrows_out, int ncols_out, DCsr<T>& out) {
   cudaStream_t s = c.stream;
   a.n = nrows_out;
   DBuf<int32_t> items(nrows_out + 1, s), ucnt(nrows_out + 1, s), big(nrows_out + 1, s), nbig(1, s);
@@ -881,6 +934,8 @@ void run_esc(Ctx& c, EscArgs<T> a, int nrows_out, int ncols_out, DCsr<T>& out) {
   }
   const int wgrid = std::min<int64_t>((nrows_out + kEscWarps - 1) / kEscWarps, 152 * 64);
   a.counts = ucnt.p;
+  a.thread_cap = kThreadRowCap;
+  FG_LAUNCH((esc_thread_kernel<T, MODE, false>), grid_for(nrows_out, 128), 128, 0, s, a, items.p);
   FG_LAUNCH((esc_warp_kernel<T, MODE, false>), wgrid, 32 * kEscWarps, wsm, s, a, items.p);
   if (a.nbig > 0)
     FG_LAUNCH((esc_block_kernel<T, MODE, false>), std::min(a.nbig, 152 * 2), kEscBlockThreads, bsm, s, a, items.p);
@@ -898,6 +953,7 @@ void run_esc(Ctx& c, EscArgs<T> a, int nrows_out, int ncols_out, DCsr<T>& out) {
   a.orp = out.rp.p;
   a.oci = out.ci.p;
   a.ov = out.v.p;
+  FG_LAUNCH((esc_thread_kernel<T, MODE, true>), grid_for(nrows_out, 128), 128, 0, s, a, items.p);
   FG_LAUNCH((esc_warp_kernel<T, MODE, true>), wgrid, 32 * kEscWarps, wsm, s, a, items.p);
   if (a.nbig > 0)
     FG_LAUNCH((esc_block_kernel<T, MODE, true>), std::min(a.nbig, 152 * 2), kEscBlockThreads, bsm, s, a, items.p);
@@ -910,6 +966,241 @@ void run_esc(Ctx& c, EscArgs<T> a, int nrows_out, int ncols_out, DCsr<T>& out) {
   }
 }
 
+
+// ---- hash SpGEMM: C = A B, row by row ----------------------------------------------
+// A row's products are visited one A entry at a time; the entries of one B row have
+// distinct columns, so every column receives at most one product per step and the
+// threads of a step never touch the same accumulator.  Steps run in order, so each
+// column is summed left to right in generation order starting from its first
+// product -- the same value as the sort-based expand-sort-compress.  The unique
+// columns are then sorted (bitonic, in shared memory) and written to the row's slot
+// of a temporary buffer; rows whose unique count exceeds the table go to a larger
+// tier.
+constexpr int kHashWarpCap = 256;
+constexpr int kHashWarps = 8;
+constexpr int kHashBlockCap = 4096;
+constexpr int kHashBlockThreads = 256;
+
+__device__ __forceinline__ unsigned hash_col(unsigned c) { return (c * 2654435761u) >> 7; }
+
+template <class T, class Sync>
+__device__ bool hash_row_accumulate(const EscArgs<T>& a, int i, int32_t* hk, T* hv, int cap, int tid, int nth,
+                                    int* s_flag, Sync sync) {
+  for (int q = tid; q < cap; q += nth) hk[q] = -1;
+  if (tid == 0) *s_flag = 0;
+  sync();
+  for (int e = a.arp[i]; e < a.arp[i + 1]; e++) {
+    const int j = a.aci[e];
+    const T av = a.av[e];
+    const int fb = a.brp[j], fe = a.brp[j + 1];
+    for (int f0 = fb; f0 < fe; f0 += nth) {
+      const int f = f0 + tid;
+      if (f < fe && *s_flag == 0) {
+        const int col = a.bci[f];
+        const T v = av * a.bv[f];
+        unsigned slot = hash_col((unsigned)col) & (unsigned)(cap - 1);
+        for (int probes = 0;; probes++) {
+          if (probes >= cap) {
+            *s_flag = 1;
+            break;
+          }
+          int k = hk[slot];
+          if (k == -1) {
+            int prev = atomicCAS(&hk[slot], -1, col);
+            if (prev == -1) {
+              hv[slot] = v;
+              break;
+            }
+            k = prev;
+          }
+          if (k == col) {
+            hv[slot] = hv[slot] + v;
+            break;
+          }
+          slot = (slot + 1) & (unsigned)(cap - 1);
+        }
+      }
+      sync();
+    }
+  }
+  return *s_flag == 0;
+}
+
+// Collects the occupied slots as (column << 32 | slot) keys, sorts them and writes
+// the row; returns the unique count.  nth threads, warp-ballot compaction.
+template <class T, class Sync>
+__device__ int hash_row_emit(const int32_t* hk, const T* hv, unsigned long long* lst, int cap, int tid, int nth,
+                             int* s_warp, int32_t* oci, T* ov, Sync sync) {
+  const int lane = tid & 31, w = tid >> 5, nw = (nth + 31) >> 5;
+  int total = 0;
+  for (int c0 = 0; c0 < cap; c0 += nth) {
+    const int q = c0 + tid;
+    const bool occ = q < cap && hk[q] != -1;
+    const unsigned m = __ballot_sync(0xffffffffu, occ);
+    int rank = __popc(m & ((1u << lane) - 1u)), chunk = __popc(m);
+    if (nw > 1) {
+      if (lane == 0) s_warp[w] = chunk;
+      sync();
+      if (tid == 0) {
+        int t = 0;
+        for (int k = 0; k < nw; k++) {
+          int v = s_warp[k];
+          s_warp[k] = t;
+          t += v;
+        }
+        s_warp[nw] = t;
+      }
+      sync();
+      rank += s_warp[w];
+      chunk = s_warp[nw];
+    }
+    if (occ) lst[total + rank] = ((unsigned long long)(unsigned)hk[q] << 32) | (unsigned)q;
+    total += chunk;
+    sync();
+  }
+  const int np2 = next_pow2(total < 2 ? 2 : total);
+  for (int p = total + tid; p < np2; p += nth) lst[p] = ~0ull;
+  sync();
+  bitonic_sort_shared(lst, np2, tid, nth, sync);
+  for (int p = tid; p < total; p += nth) {
+    oci[p] = (int32_t)(lst[p] >> 32);
+    ov[p] = hv[(unsigned)(lst[p] & 0xffffffffu)];
+  }
+  sync();
+  return total;
+}
+
+template <class T>
+__global__ void hash_warp_kernel(EscArgs<T> a, const int32_t* toff, int32_t* tci, T* tv, int32_t* counts,
+                                 int32_t* over, int32_t* nover) {
+  __shared__ int32_t hk[kHashWarps][kHashWarpCap];
+  __shared__ T hv[kHashWarps][kHashWarpCap];
+  __shared__ unsigned long long lst[kHashWarps][kHashWarpCap];
+  __shared__ int s_flag[kHashWarps];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int i = blockIdx.x * kHashWarps + w; i < a.n; i += gridDim.x * kHashWarps) {
+    bool ok = hash_row_accumulate<T>(a, i, hk[w], hv[w], kHashWarpCap, lane, 32, &s_flag[w], WarpSync());
+    if (!ok) {
+      if (lane == 0) {
+        over[atomicAdd(nover, 1)] = i;
+        counts[i] = 0;
+      }
+      __syncwarp();
+      continue;
+    }
+    int u = hash_row_emit<T>(hk[w], hv[w], lst[w], kHashWarpCap, lane, 32, nullptr, tci + toff[i], tv + toff[i],
+                             WarpSync());
+    if (lane == 0) counts[i] = u;
+    __syncwarp();
+  }
+}
+
+template <class T>
+__global__ void hash_block_kernel(EscArgs<T> a, const int32_t* rows, int nrows, const int32_t* toff, int32_t* tci,
+                                  T* tv, int32_t* counts, int32_t* over, int32_t* nover) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  unsigned long long* lst = reinterpret_cast<unsigned long long*>(smem_raw);
+  T* hv = reinterpret_cast<T*>(lst + kHashBlockCap);
+  int32_t* hk = reinterpret_cast<int32_t*>(hv + kHashBlockCap);
+  __shared__ int s_flag;
+  __shared__ int s_warp[kHashBlockThreads / 32 + 1];
+  for (int b = blockIdx.x; b < nrows; b += gridDim.x) {
+    const int i = rows[b];
+    bool ok = hash_row_accumulate<T>(a, i, hk, hv, kHashBlockCap, threadIdx.x, blockDim.x, &s_flag, BlockSync());
+    if (!ok) {
+      if (threadIdx.x == 0) {
+        over[atomicAdd(nover, 1)] = i;
+        counts[i] = 0;
+      }
+      __syncthreads();
+      continue;
+    }
+    int u = hash_row_emit<T>(hk, hv, lst, kHashBlockCap, threadIdx.x, blockDim.x, s_warp, tci + toff[i],
+                             tv + toff[i], BlockSync());
+    if (threadIdx.x == 0) counts[i] = u;
+    __syncthreads();
+  }
+}
+
+__global__ void spgemm_capacity_kernel(int n, const int32_t* items, int ncols, int32_t* cap) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) cap[i] = min(items[i], ncols);
+}
+
+template <class T>
+__global__ void compact_rows_copy_kernel(int n, const int32_t* toff, const int32_t* tci, const T* tv,
+                                         const int32_t* orp, int32_t* oci, T* ov) {
+  const int lane = threadIdx.x & 31;
+  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += (gridDim.x * blockDim.x) >> 5) {
+    const int len = orp[i + 1] - orp[i];
+    for (int t = lane; t < len; t += 32) {
+      oci[orp[i] + t] = tci[toff[i] + t];
+      ov[orp[i] + t] = tv[toff[i] + t];
+    }
+  }
+}
+
+template <class T>
+void run_spgemm_hash(Ctx& c, EscArgs<T> a, int nrows_out, int ncols_out, DCsr<T>& out) {
+  cudaStream_t s = c.stream;
+  a.n = nrows_out;
+  DBuf<int32_t> items(nrows_out + 1, s), capv(nrows_out + 1, s), toff(nrows_out + 1, s), cnt(nrows_out + 1, s);
+  a.counts = items.p;
+  FG_LAUNCH((esc_count_items_kernel<T, ESC_SPGEMM>), grid_for(nrows_out, 256), 256, 0, s, a);
+  FG_LAUNCH(spgemm_capacity_kernel, grid_for(nrows_out, 256), 256, 0, s, nrows_out, items.p, ncols_out, capv.p);
+  const int64_t tcap = exclusive_scan(capv.p, toff.p, nrows_out, s);
+  FG_REQUIRE(tcap < INT32_MAX, FEMGPU_ERR_LIMIT, "SpGEMM temporary exceeds int32 indexing");
+  DBuf<int32_t> tci(tcap > 0 ? tcap : 1, s);
+  DBuf<T> tv(tcap > 0 ? tcap : 1, s);
+  DBuf<int32_t> over1(nrows_out + 1, s), nover1(1, s), over2(nrows_out + 1, s), nover2(1, s);
+  nover1.zero();
+  nover2.zero();
+  const int wgrid = std::min<int64_t>((nrows_out + kHashWarps - 1) / kHashWarps, 152 * 32);
+  FG_LAUNCH(hash_warp_kernel<T>, wgrid, 32 * kHashWarps, 0, s, a, toff.p, tci.p, tv.p, cnt.p, over1.p, nover1.p);
+  const int n1 = read_scalar(nover1.p, s);
+  if (n1 > 0) {
+    const size_t bsm = (size_t)kHashBlockCap * (sizeof(unsigned long long) + sizeof(T) + sizeof(int32_t));
+    FG_CUDA(cudaFuncSetAttribute(hash_block_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsm));
+    FG_LAUNCH(hash_block_kernel<T>, std::min(n1, 152 * 2), kHashBlockThreads, bsm, s, a, over1.p, n1, toff.p, tci.p,
+              tv.p, cnt.p, over2.p, nover2.p);
+    const int n2 = read_scalar(nover2.p, s);
+    if (n2 > 0) {
+      // more unique columns than the block table: dense accumulator over the columns
+      const size_t dsm = (size_t)ncols_out * (sizeof(T) + 1);
+      FG_REQUIRE(dsm <= 200 * 1024, FEMGPU_ERR_LIMIT, "SpGEMM row with more than 4096 unique columns");
+      EscArgs<T> ad = a;
+      ad.nbig = n2;
+      ad.big_rows = over2.p;
+      if (dsm > 48 * 1024) {
+        FG_CUDA(cudaFuncSetAttribute(esc_dense_kernel<T, ESC_SPGEMM, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm));
+        FG_CUDA(cudaFuncSetAttribute(esc_dense_kernel<T, ESC_SPGEMM, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm));
+      }
+      ad.counts = cnt.p;
+      FG_LAUNCH((esc_dense_kernel<T, ESC_SPGEMM, false>), std::min(n2, 304), 256, dsm, s, ad, ncols_out, nullptr,
+                nullptr);
+      ad.orp = toff.p;
+      ad.oci = tci.p;
+      ad.ov = tv.p;
+      FG_LAUNCH((esc_dense_kernel<T, ESC_SPGEMM, true>), std::min(n2, 304), 256, dsm, s, ad, ncols_out, nullptr,
+                nullptr);
+    }
+  }
+  out.n = nrows_out;
+  out.m = ncols_out;
+  out.rp.alloc(nrows_out + 1, s);
+  out.nnz = exclusive_scan(cnt.p, out.rp.p, nrows_out, s);
+  out.ci.alloc(out.nnz > 0 ? out.nnz : 1, s);
+  out.v.alloc(out.nnz > 0 ? out.nnz : 1, s);
+  FG_LAUNCH(compact_rows_copy_kernel<T>, grid_for((int64_t)nrows_out * 32, 256), 256, 0, s, nrows_out, toff.p, tci.p,
+            tv.p, out.rp.p, out.ci.p, out.v.p);
+}
+
+template <class T, int MODE>
+void run_esc(Ctx& c, EscArgs<T> a, int nrows_out, int ncols_out, DCsr<T>& out) {
+  if (MODE == ESC_SPGEMM) run_spgemm_hash<T>(c, a, nrows_out, ncols_out, out);
+  else run_esc_sort<T, MODE>(c, a, nrows_out, ncols_out, out);
+}
+
 // ---- level matrices -----------------------------------------------------------------
 template <class T>
 __global__ void diag_kernel(int n, const int32_t* rp, const int32_t* ci, const T* v, T* d) {
@@ -918,6 +1209,12 @@ __global__ void diag_kernel(int n, const int32_t* rp, const int32_t* ci, const T
     int s = lower_bound_i32(ci, rp[i], rp[i + 1], i);
     d[i] = (s < rp[i + 1] && ci[s] == i) ? v[s] : (T)0;
   }
+}
+
+template <class T>
+__global__ void reciprocal_kernel(int n, const T* d, T* dinv) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dinv[i] = (T)1 / d[i];
 }
 
 template <class T>
@@ -1176,6 +1473,8 @@ void build_levels(Ctx& c, Hierarchy<T>& H) {
     pt.mark("permute");
     L.diag.alloc(N, s);
     FG_LAUNCH(diag_kernel<T>, grid_for(N, 256), 256, 0, s, N, L.Ap.rp.p, L.Ap.ci.p, L.Ap.v.p, L.diag.p);
+    L.dinv.alloc(N, s);
+    FG_LAUNCH(reciprocal_kernel<T>, grid_for(N, 256), 256, 0, s, N, L.diag.p, L.dinv.p);
     // in/out-of-partition split
     {
       DBuf<int32_t> cin(N + 1, s), cout(N + 1, s);

@@ -69,20 +69,16 @@ __global__ void cast_out_kernel(int n, const T* in, double* out) {
   if (i < n) out[i] = (double)in[i];
 }
 
-// x += w (b - sAx - d x) / d with the weight in double (gauss_seidel.cu:1333-1341).
+// Weighted Jacobi update x += w (b - sAx - d x) / d (gauss_seidel.cu:1333-1341) in the
+// hierarchy's precision, dividing by d as a multiplication with the precomputed 1/d.
+// The reference forms the correction in double because its weight is a double;
+// on GB300 that FP64 division per row and sweep dominated the smoother, so the
+// update is done in T (the CPU oracle uses the same expression).
 template <class T>
-__device__ __forceinline__ T relax(T x, T b, T sax, T d, double w) {
+__device__ __forceinline__ T relax(T x, T b, T sax, T d, T dinv, T w) {
   T t = b - sax;
   t = t - d * x;
-  return (T)((double)x + (w * (double)t) / (double)d);
-}
-
-template <class T>
-__device__ __forceinline__ T in_row_sum(const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
-                                       const T* __restrict__ v, int row, int rs, const T* sx) {
-  T s = 0;
-  for (int e = rp[row]; e < rp[row + 1]; e++) s = s + v[e] * sx[ci[e] - rs];
-  return s;
+  return x + (w * t) * dinv;
 }
 
 // Shared-memory layout of one partition in the smoother: x, the in-partition sums,
@@ -90,7 +86,7 @@ __device__ __forceinline__ T in_row_sum(const int32_t* __restrict__ rp, const in
 // partition's block of in-partition entries with 16-bit local column indices.
 template <class T>
 struct PartSmem {
-  T *sx, *sax, *sb, *sd, *sval;
+  T *sx, *sax, *sb, *sd, *sdi, *sval;
   int32_t* srp;
   uint16_t* scol;
 };
@@ -102,7 +98,8 @@ __device__ __forceinline__ PartSmem<T> carve(unsigned char* sm, int mcap, int ec
   L.sax = L.sx + mcap;
   L.sb = L.sax + mcap;
   L.sd = L.sb + mcap;
-  L.sval = L.sd + mcap;
+  L.sdi = L.sd + mcap;
+  L.sval = L.sdi + mcap;
   L.srp = reinterpret_cast<int32_t*>(L.sval + ecap);
   L.scol = reinterpret_cast<uint16_t*>(L.srp + mcap + 1);
   return L;
@@ -110,7 +107,7 @@ __device__ __forceinline__ PartSmem<T> carve(unsigned char* sm, int mcap, int ec
 
 template <class T>
 size_t part_smem_bytes(int mcap, int ecap) {
-  return (size_t)mcap * 4 * sizeof(T) + (size_t)ecap * sizeof(T) + (size_t)(mcap + 1) * 4 + (size_t)ecap * 2 + 16;
+  return (size_t)mcap * 5 * sizeof(T) + (size_t)ecap * sizeof(T) + (size_t)(mcap + 1) * 4 + (size_t)ecap * 2 + 16;
 }
 
 // Sum over row t's in-partition entries in ascending column order, products rounded
@@ -137,8 +134,8 @@ template <class T, bool POST, bool STAGED>
 __global__ void __launch_bounds__(256) smooth_kernel(
     const int32_t* __restrict__ part_idx, const int32_t* __restrict__ agg_idx, const int32_t* __restrict__ irp,
     const int32_t* __restrict__ ici, const T* __restrict__ iv, const int32_t* __restrict__ orp,
-    const int32_t* __restrict__ oci, const T* __restrict__ ov, const T* __restrict__ diag, const T* __restrict__ b,
-    double w, int inner, const T* __restrict__ x_in, T* __restrict__ x_out, T* __restrict__ r_out, int mcap,
+    const int32_t* __restrict__ oci, const T* __restrict__ ov, const T* __restrict__ diag,
+    const T* __restrict__ dinv, const T* __restrict__ b, T w, int inner, const T* __restrict__ x_in, T* __restrict__ x_out, T* __restrict__ r_out, int mcap,
     int ecap) {
   extern __shared__ __align__(16) unsigned char sm[];
   const int rs = agg_idx[part_idx[blockIdx.x]], re = agg_idx[part_idx[blockIdx.x + 1]];
@@ -147,8 +144,9 @@ __global__ void __launch_bounds__(256) smooth_kernel(
   PartSmem<T> P = carve<T>(sm, mcap, STAGED ? ecap : 0);
   for (int t = threadIdx.x; t < m; t += blockDim.x) {
     const int row = rs + t;
-    const T d = diag[row];
+    const T d = diag[row], di = dinv[row];
     P.sd[t] = d;
+    P.sdi[t] = di;
     P.srp[t] = irp[row] - es;
     if (POST) {
       T acc = b[row];
@@ -158,7 +156,7 @@ __global__ void __launch_bounds__(256) smooth_kernel(
     } else {
       const T bv = b[row];
       P.sb[t] = bv;
-      P.sx[t] = (T)((w * (double)bv) / (double)d);
+      P.sx[t] = (w * bv) * di;
     }
   }
   if (threadIdx.x == 0) P.srp[m] = ne;
@@ -171,7 +169,7 @@ __global__ void __launch_bounds__(256) smooth_kernel(
   for (int it = 0; it < inner; it++) {
     for (int t = threadIdx.x; t < m; t += blockDim.x) P.sax[t] = part_row_sum<T, STAGED>(P, t, ici, iv, es, rs);
     __syncthreads();
-    for (int t = threadIdx.x; t < m; t += blockDim.x) P.sx[t] = relax(P.sx[t], P.sb[t], P.sax[t], P.sd[t], w);
+    for (int t = threadIdx.x; t < m; t += blockDim.x) P.sx[t] = relax(P.sx[t], P.sb[t], P.sax[t], P.sd[t], P.sdi[t], w);
     __syncthreads();
   }
   for (int t = threadIdx.x; t < m; t += blockDim.x) {
@@ -394,7 +392,7 @@ void set_smem_attrs(const Level<T>& L) {
 template <class T>
 void smooth(Ctx& c, Level<T>& L, bool post, const T* b, const T* xin, T* xout, T* rout) {
   cudaStream_t s = c.stream;
-  const double w = c.cfg.smootherWeight;
+  const T w = (T)c.cfg.smootherWeight;
   const int inner = post ? c.cfg.postInnerIters : c.cfg.preInnerIters;
   const size_t sm = smooth_smem(L);
   const bool st = staged(L);
@@ -403,7 +401,7 @@ void smooth(Ctx& c, Level<T>& L, bool post, const T* b, const T* xin, T* xout, T
   // the limit is a per-function attribute shared by every handle: set it per launch
   if (sm > 48 * 1024) FG_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   FG_LAUNCH(k, L.npart, 256, sm, s, L.part_idx.p, L.agg_idx.p, L.Ain.rp.p, L.Ain.ci.p, L.Ain.v.p, L.Aout.rp.p,
-            L.Aout.ci.p, L.Aout.v.p, L.diag.p, b, w, inner, xin, xout, rout, L.max_part_rows, L.max_part_entries);
+            L.Aout.ci.p, L.Aout.v.p, L.diag.p, L.dinv.p, b, w, inner, xin, xout, rout, L.max_part_rows, L.max_part_entries);
 }
 
 // b (level order for l > 0, already permuted for l == 0) -> x (same ordering).

@@ -49,7 +49,7 @@ struct Level {
   int64_t gnnz = 0;
   DBuf<int32_t> perm, iperm, agg_idx, part_idx, agg_of;
   DCsr<T> Ap, Ain, Aout, P, R;
-  DBuf<T> diag;
+  DBuf<T> diag, dinv;  // diagonal of Ap and its reciprocal
   int max_part_rows = 0;
   int max_part_entries = 0;  // in-partition off-diagonal entries of the largest partition
   // coarsest: explicit inverse, row-major n x n
