@@ -232,26 +232,25 @@ def main():
            "d2h_bytes_per_step": 8 * n}
     clk = clocks.stop()
 
-    # ---- roofline: FP64 CSR SpMV of the outer PCG (CUDA events on the solver's stream)
+    # ---- rooflines: each hot kernel of a PCG iteration timed with CUDA events on the
+    # solver's stream by the library (femgpu_profile_kernel); each runs once per
+    # iteration, so the dominant one has the largest time per launch
     peak, peak_kind = peaks()
     rp, ci, _ = s.matrix()
     nnz = int(ci.shape[0])
-    y = torch.empty_like(d_x)
-    for _ in range(3):
-        s.spmv_device(d_x.data_ptr(), y.data_ptr())
-    reps = 20
-    a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    a0.record(stream)
-    for _ in range(reps):
-        s.spmv_device(d_x.data_ptr(), y.data_ptr())
-    a1.record(stream)
-    torch.cuda.synchronize()
-    spmv_ms = a0.elapsed_time(a1) / reps
-    spmv_bytes = 12 * nnz + 4 * (n + 1) + 8 * n + 8 * n
-    achieved = spmv_bytes / (spmv_ms / 1e3) / 1e9
-    roofline = {"bound": "hbm", "kernel": "spmv_kernel (FP64 CSR, outer PCG)", "achieved": round(achieved, 1),
-                "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
-                "peak_source": peak_kind, "algorithmic_bytes": spmv_bytes, "ms": round(spmv_ms, 4)}
+    traffic = {}
+    tpath = os.path.join(ROOT, "profiles", "dram_traffic_128cube.json")
+    if os.path.exists(tpath):
+        with open(tpath) as fh:
+            traffic = json.load(fh)
+    rooflines = []
+    for which, name in femgpu.Solver.KERNELS.items():
+        kms, kbytes = s.profile_kernel(which, reps=20)
+        ach = kbytes / (kms / 1e3) / 1e9
+        rooflines.append({"bound": "hbm", "kernel": name, "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+                          "frac": round(ach / peak, 4), "traffic": traffic.get(name), "peak_source": peak_kind,
+                          "algorithmic_bytes": kbytes, "ms": round(kms, 4)})
+    roofline = max(rooflines, key=lambda r: r["ms"])
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -271,7 +270,8 @@ def main():
                           "l2": "inputs larger than L2 (A: %.0f MB)" % (12 * nnz / 1e6)},
                "pcg_iterations": iters[-1], "relres": relres, "setup_ms": float(np.mean(setup_ms)),
                "solve_ms": float(np.mean(solve_ms)), "assembly_ms": assembly_ms,
-               "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu,
+               "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "rooflines": rooflines,
+               "cpu_baseline": cpu,
                "clocks": clk}
         print(json.dumps(out))
     if dist:

@@ -163,6 +163,12 @@ femgpu_status femgpu_level_get(femgpu_handle h, int level, int32_t* A_rowptr, in
                                int32_t* P_rowptr, int32_t* P_cols, double* P_vals);
 /* One V-cycle z = M r on host vectors (AMG_Level::cycle_level0, amg_level.cu:74-128). */
 femgpu_status femgpu_vcycle(femgpu_handle h, const double* r, double* z);
+/* Times one hot kernel of the current hierarchy with CUDA events on the handle's
+ * stream (3 untimed launches, then `reps`) and reports its average time and its
+ * algorithmic bytes per launch: 0 = outer PCG FP64 SpMV (+ dot), 1 = level-0
+ * pre-smoother, 2 = level-0 post-smoother relax, 3 = level-0 restriction,
+ * 4 = level-0 prolongation.  No reference counterpart (measurement support). */
+femgpu_status femgpu_profile_kernel(femgpu_handle h, int which, int reps, double* avg_ms, double* bytes);
 /* Number of kernel launches issued by the library on this handle so far. */
 femgpu_status femgpu_kernel_launches(femgpu_handle h, int64_t* count);
 

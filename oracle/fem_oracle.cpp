@@ -800,9 +800,12 @@ struct LevelBase {
   virtual ~LevelBase() {}
 };
 
+int lanes_for_rows(int64_t nnz, int n);
+
 template <class T>
 struct Level {
   int n = 0;
+  int smooth_lanes = 1; /* lanes per row of the in-partition sums (device layout rule) */
   Csr<T> A;          /* level matrix, level's own numbering */
   bool coarsest = false;
   /* aggregation (non-coarsest) */
@@ -1128,6 +1131,15 @@ int setup_levels(orc_amg* h, std::vector<Level<T>>& L, const Csr<double>& A, con
     lv.dinv.resize(N);
     for (int i = 0; i < N; i++) lv.dinv[i] = (T)1 / lv.diag[i];
     split_partitions(lv);
+    {
+      /* the device keeps rows of <= 16 in-partition entries in registers (one lane per
+       * row) when partitions have <= 1024 rows, else sums rows with S lanes */
+      int max_row = 0, max_part = 0;
+      for (int i = 0; i < N; i++) max_row = std::max(max_row, lv.Ain.rp[i + 1] - lv.Ain.rp[i]);
+      for (size_t q = 0; q + 1 < lv.partIdx.size(); q++)
+        max_part = std::max(max_part, lv.aggIdx[lv.partIdx[q + 1]] - lv.aggIdx[lv.partIdx[q]]);
+      lv.smooth_lanes = (max_row <= 16 && max_part <= 1024) ? 1 : lanes_for_rows(lv.Ain.nnz(), N);
+    }
     lv.P = build_prolongator(lv.Ap, lv.diag, lv.aggOf, nagg, c.pro_omega);
     lv.R = transpose(lv.P);
     Csr<T> AP = spgemm(lv.Ap, lv.P);
@@ -1159,6 +1171,23 @@ inline T relax_update(T x, T b, T sAx, T d, T dinv, T w) {
   return x + (w * t) * dinv;
 }
 
+/* Row sum of in-partition entries in the device's lane order: S lanes, lane j takes
+ * entries j, j+S, ... (products rounded, then added), then an xor butterfly. */
+template <class T>
+inline T part_row_sum(const Csr<T>& M, int i, const T* x, int xoff, int S) {
+  T p[32], q[32];
+  for (int j = 0; j < S; j++) p[j] = 0;
+  for (int e = M.rp[i]; e < M.rp[i + 1]; e++) {
+    int j = (e - M.rp[i]) % S;
+    p[j] = p[j] + M.v[e] * x[M.ci[e] - xoff];
+  }
+  for (int off = S >> 1; off > 0; off >>= 1) {
+    for (int j = 0; j < S; j++) q[j] = p[j] + p[j ^ off];
+    for (int j = 0; j < S; j++) p[j] = q[j];
+  }
+  return p[0];
+}
+
 template <class T>
 void pre_smooth(Level<T>& L, const orc_config& c) {
   int np = (int)L.partIdx.size() - 1;
@@ -1172,16 +1201,11 @@ void pre_smooth(Level<T>& L, const orc_config& c) {
       sAx.assign(re - rs, (T)0);
       for (int i = rs; i < re; i++) L.x[i] = (w * L.b[i]) * L.dinv[i];
       for (int it = 0; it < c.pre_inner; it++) {
-        for (int i = rs; i < re; i++) {
-          T s = 0;
-          for (int e = L.Ain.rp[i]; e < L.Ain.rp[i + 1]; e++) s = s + L.Ain.v[e] * L.x[L.Ain.ci[e]];
-          sAx[i - rs] = s;
-        }
+        for (int i = rs; i < re; i++) sAx[i - rs] = part_row_sum(L.Ain, i, L.x.data(), 0, L.smooth_lanes);
         for (int i = rs; i < re; i++) L.x[i] = relax_update(L.x[i], L.b[i], sAx[i - rs], L.diag[i], L.dinv[i], w);
       }
       for (int i = rs; i < re; i++) {
-        T s = 0;
-        for (int e = L.Ain.rp[i]; e < L.Ain.rp[i + 1]; e++) s = s + L.Ain.v[e] * L.x[L.Ain.ci[e]];
+        T s = part_row_sum(L.Ain, i, L.x.data(), 0, L.smooth_lanes);
         T t = L.b[i] - s;
         L.r[i] = t - L.diag[i] * L.x[i];
       }
@@ -1218,11 +1242,7 @@ void post_smooth(Level<T>& L, const orc_config& c) {
           sx[i - rs] = L.x[i];
         }
         for (int it = 0; it < c.post_inner; it++) {
-          for (int i = rs; i < re; i++) {
-            T s = 0;
-            for (int e = L.Ain.rp[i]; e < L.Ain.rp[i + 1]; e++) s = s + L.Ain.v[e] * sx[L.Ain.ci[e] - rs];
-            sAx[i - rs] = s;
-          }
+          for (int i = rs; i < re; i++) sAx[i - rs] = part_row_sum(L.Ain, i, sx.data(), rs, L.smooth_lanes);
           for (int i = rs; i < re; i++) sx[i - rs] = relax_update(sx[i - rs], sb[i - rs], sAx[i - rs], L.diag[i], L.dinv[i], w);
         }
         for (int i = rs; i < re; i++) L.xo[i] = sx[i - rs];
@@ -1269,10 +1289,15 @@ void vcycle(std::vector<Level<T>>& L, int l, const orc_config& c) {
   Level<T>& lv = L[l];
   if (lv.coarsest) { /* lv.F holds the explicit inverse */
     const int N = lv.A.n;
-    for (int i = 0; i < N; i++) {
-      double s = 0.0;
-      for (int j = 0; j < N; j++) s = fma(lv.F[(size_t)i * N + j], (double)lv.b[j], s);
-      lv.x[i] = (T)s;
+    for (int i = 0; i < N; i++) { /* the device's warp-per-row order: 32 fma lanes, butterfly */
+      double p[32], q[32];
+      for (int j = 0; j < 32; j++) p[j] = 0.0;
+      for (int j = 0; j < N; j++) p[j & 31] = fma(lv.F[(size_t)i * N + j], (double)lv.b[j], p[j & 31]);
+      for (int off = 16; off > 0; off >>= 1) {
+        for (int j = 0; j < 32; j++) q[j] = p[j] + p[j ^ off];
+        for (int j = 0; j < 32; j++) p[j] = q[j];
+      }
+      lv.x[i] = (T)p[0];
     }
     return;
   }

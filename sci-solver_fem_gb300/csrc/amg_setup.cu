@@ -446,6 +446,29 @@ __global__ void node_order_kernel(int nagg, const int32_t* old_of, const int32_t
   }
 }
 
+// Opt-in setup phase timing (environment FEMGPU_PROFILE set): synchronizes between
+// phases and prints the host wall time of each to stderr.
+struct PhaseTimer {
+  bool on;
+  cudaStream_t s;
+  int level;
+  std::chrono::steady_clock::time_point t0;
+  PhaseTimer(cudaStream_t st, int lvl) : on(getenv("FEMGPU_PROFILE") != nullptr), s(st), level(lvl) {
+    if (on) {
+      cudaStreamSynchronize(s);
+      t0 = std::chrono::steady_clock::now();
+    }
+  }
+  void mark(const char* what) {
+    if (!on) return;
+    cudaStreamSynchronize(s);
+    auto t = std::chrono::steady_clock::now();
+    fprintf(stderr, "[femgpu setup] level %d %-10s %8.3f ms\n", level, what,
+            std::chrono::duration<double, std::milli>(t - t0).count());
+    t0 = t;
+  }
+};
+
 struct OldMisOut {
   int nagg = 0, npart = 0;
   DBuf<int32_t> perm, iperm, agg_idx, part_idx, agg_of, part_of_row, xadj_out, adj_out;
@@ -457,8 +480,10 @@ void old_mis(Ctx& c, int n, const int32_t* xadj, const int32_t* adj, OldMisOut& 
   cudaStream_t s = c.stream;
   const int params = c.cfg.randMisParameters;
   const int fine_depth = params % 100, coarse_depth = (params / 100) % 100, min_agg = (params / 10000) % 10;
+  PhaseTimer pt(s, -1);
   DBuf<int32_t> fine;
   aggregate(c, n, xadj, adj, fine_depth, false, min_agg, 0, n, nullptr, fine);
+  pt.mark("fine agg");
   const int nagg = reduce_max(fine.p, n, s) + 1;
   // aggregate member lists, ascending node id
   DBuf<int32_t> acount(nagg + 1, s), astart(nagg + 1, s), cursor(nagg, s), members(n, s);
@@ -482,9 +507,11 @@ void old_mis(Ctx& c, int n, const int32_t* xadj, const int32_t* adj, OldMisOut& 
   DBuf<int32_t> iadj(innz > 0 ? innz : 1, s);
   FG_LAUNCH(compact_segments_kernel, grid_for((int64_t)nagg * 32, 256), 256, 0, s, nagg, cand.p, coff.p, ixadj.p,
             iadj.p);
+  pt.mark("induced");
   // partitions of aggregates (aggregateWeightedGraph, weights = aggregate sizes)
   DBuf<int32_t> coarse;
   aggregate(c, nagg, ixadj.p, iadj.p, coarse_depth, true, 0, c.cfg.partitionMaxSize, n, acount.p, coarse);
+  pt.mark("partitions");
   const int npart = reduce_max(coarse.p, nagg, s) + 1;
   // new aggregate ids: order (partition, old id)
   DBuf<int32_t> pcount(npart + 1, s), pcur(npart, s), old_of(nagg, s), new_id(nagg, s);
@@ -517,6 +544,7 @@ void old_mis(Ctx& c, int n, const int32_t* xadj, const int32_t* adj, OldMisOut& 
   FG_LAUNCH(node_order_kernel, grid_for(nagg, 256), 256, 0, s, nagg, old_of.p, astart.p, members.p, o.agg_idx.p,
             coarse.p, o.iperm.p, o.agg_of.p, o.part_of_row.p);
   FG_LAUNCH(invert_kernel, grid_for(n, 256), 256, 0, s, n, o.iperm.p, o.perm.p);
+  pt.mark("order");
   o.nagg = nagg;
   o.npart = npart;
 }
@@ -839,7 +867,34 @@ __global__ void collect_dense_rows_kernel(int n, const int32_t* items, int cap, 
 // ---- thread tier: short PERMUTE / PROLONG rows, one thread per row -----------------
 // Items are generated in order and merged into a sorted local list; a repeated
 // column adds to its running sum (left to right from the first item).
-constexpr int kThreadRowCap = 32;
+constexpr int kThreadRowCap = 16;
+
+// Bitonic network on N register-resident (key, value) pairs; every index is a
+// compile-time constant after unrolling, so nothing spills to local memory.
+template <class T, int N>
+__device__ __forceinline__ void sort_network(unsigned long long (&k)[N], T (&v)[N]) {
+#pragma unroll
+  for (int size = 2; size <= N; size <<= 1) {
+#pragma unroll
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+#pragma unroll
+      for (int i = 0; i < N; i++) {
+        const int j = i ^ stride;
+        if (j > i) {
+          const bool asc = (i & size) == 0;
+          if ((k[i] > k[j]) == asc) {
+            unsigned long long tk = k[i];
+            k[i] = k[j];
+            k[j] = tk;
+            T tv = v[i];
+            v[i] = v[j];
+            v[j] = tv;
+          }
+        }
+      }
+    }
+  }
+}
 
 template <class T, int MODE, bool WRITE>
 __global__ void esc_thread_kernel(EscArgs<T> a, const int32_t* items) {
@@ -847,46 +902,67 @@ __global__ void esc_thread_kernel(EscArgs<T> a, const int32_t* items) {
   if (i >= a.n) return;
   const int len = items[i];
   if (len > kThreadRowCap) return;
-  int cols[kThreadRowCap];
-  T vals[kThreadRowCap];
-  int u = 0;
-  auto add = [&](int col, T v) {
-    int p = u;
-    while (p > 0 && cols[p - 1] > col) p--;
-    if (p > 0 && cols[p - 1] == col) {
-      vals[p - 1] = vals[p - 1] + v;
-      return;
-    }
-    for (int q = u; q > p; q--) {
-      cols[q] = cols[q - 1];
-      vals[q] = vals[q - 1];
-    }
-    cols[p] = col;
-    vals[p] = v;
-    u++;
-  };
+  unsigned long long key[kThreadRowCap];
+  T val[kThreadRowCap];
   const int r = esc_input_row<T, MODE>(a, i);
-  for (int q = a.arp[r]; q < a.arp[r + 1]; q++) {
-    const int j = a.aci[q];
-    if (MODE == ESC_PERMUTE) {
-      add(a.perm ? a.perm[j] : j, a.av[q]);
+  const int rb = a.arp[r], re = a.arp[r + 1];
+#pragma unroll
+  for (int g = 0; g < kThreadRowCap; g++) {
+    key[g] = ~0ull;
+    val[g] = (T)0;
+    const int q = rb + g;
+    if (q < re) {
+      const int j = a.aci[q];
+      int col;
+      T v;
+      if (MODE == ESC_PERMUTE) {
+        col = a.perm ? a.perm[j] : j;
+        v = a.av[q];
+      } else {
+        col = a.agg_of[j];
+        T t = (a.neg_omega * a.av[q]) * (T)1;
+        v = t / a.diag[i];
+      }
+      key[g] = ((unsigned long long)(unsigned)col << 32) | (unsigned)g;
+      val[g] = v;
+    } else if (MODE == ESC_PROLONG && q == re) {
+      key[g] = ((unsigned long long)(unsigned)a.agg_of[i] << 32) | (unsigned)g;
+      val[g] = (T)1;
+    }
+  }
+  sort_network<T, kThreadRowCap>(key, val);
+  // runs of equal columns summed left to right (generation order within the run)
+  const int o = WRITE ? a.orp[i] : 0;
+  int u = 0;
+  unsigned cur = 0xffffffffu;
+  T sum = (T)0;
+#pragma unroll
+  for (int g = 0; g < kThreadRowCap; g++) {
+    if (key[g] == ~0ull) continue;
+    const unsigned col = (unsigned)(key[g] >> 32);
+    if (col != cur) {
+      if (cur != 0xffffffffu) {
+        if (WRITE) {
+          a.oci[o + u] = (int32_t)cur;
+          a.ov[o + u] = sum;
+        }
+        u++;
+      }
+      cur = col;
+      sum = val[g];
     } else {
-      T t = (a.neg_omega * a.av[q]) * (T)1;
-      add(a.agg_of[j], t / a.diag[i]);
+      sum = sum + val[g];
     }
   }
-  if (MODE == ESC_PROLONG) add(a.agg_of[i], (T)1);
-  if (WRITE) {
-    const int o = a.orp[i];
-    for (int q = 0; q < u; q++) {
-      a.oci[o + q] = cols[q];
-      a.ov[o + q] = vals[q];
+  if (cur != 0xffffffffu) {
+    if (WRITE) {
+      a.oci[o + u] = (int32_t)cur;
+      a.ov[o + u] = sum;
     }
-  } else {
-    a.counts[i] = u;
+    u++;
   }
+  if (!WRITE) a.counts[i] = u;
 }
-
 
 template <class T, int MODE>
 void run_esc_sort(Ctx& c, EscArgs<T> a, int nrows_out, int ncols_out, DCsr<T>& out) {
@@ -1070,16 +1146,111 @@ __device__ int hash_row_emit(const int32_t* hk, const T* hv, unsigned long long*
   return total;
 }
 
+// Warp tier: 32 products per step in generation order (A entries of the row taken 32
+// at a time, their B rows flattened by a warp scan).  Lanes holding the same column
+// are grouped with __match_any_sync; the group's lowest lane adds the group's
+// products to the accumulator in lane order, so each column is still summed left
+// to right in generation order.
+template <class T>
+__device__ bool hash_row_accumulate_matched(const EscArgs<T>& a, int i, int32_t* hk, T* hv, T* sv, int cap,
+                                            int lane, int* s_flag) {
+  for (int q = lane; q < cap; q += 32) hk[q] = -1;
+  if (lane == 0) *s_flag = 0;
+  __syncwarp();
+  const int rb = a.arp[i], re = a.arp[i + 1];
+  for (int eb = rb; eb < re; eb += 32) {
+    const int e = eb + lane;
+    int j = 0, len = 0;
+    T av = (T)0;
+    if (e < re) {
+      j = a.aci[e];
+      av = a.av[e];
+      len = a.brp[j + 1] - a.brp[j];
+    }
+    int incl = len;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    const int jb = e < re ? a.brp[j] : 0;
+    for (int g0 = 0; g0 < total; g0 += 32) {
+      const int g = g0 + lane;
+      const bool live = g < total;
+      int owner = 0;
+#pragma unroll
+      for (int st = 16; st > 0; st >>= 1) {
+        int probe = __shfl_sync(0xffffffffu, incl, owner + st - 1);
+        if (probe <= g) owner += st;
+      }
+      owner = owner > 31 ? 31 : owner;
+      const int o_incl = __shfl_sync(0xffffffffu, incl, owner);
+      const int o_len = __shfl_sync(0xffffffffu, len, owner);
+      const int o_jb = __shfl_sync(0xffffffffu, jb, owner);
+      const T o_av = __shfl_sync(0xffffffffu, av, owner);
+      int col = -1;
+      T v = (T)0;
+      if (live) {
+        const int f = o_jb + (g - (o_incl - o_len));
+        col = a.bci[f];
+        v = o_av * a.bv[f];
+      }
+      sv[lane] = v;
+      const unsigned peers = __match_any_sync(0xffffffffu, col);
+      __syncwarp();
+      const bool leader = live && (__ffs(peers) - 1) == lane;
+      if (leader && *s_flag == 0) {
+        unsigned slot = hash_col((unsigned)col) & (unsigned)(cap - 1);
+        int found = -1;
+        bool fresh = false;
+        for (int probes = 0; probes < cap; probes++) {
+          int k = hk[slot];
+          if (k == -1) {
+            int prev = atomicCAS(&hk[slot], -1, col);
+            if (prev == -1) {
+              found = (int)slot;
+              fresh = true;
+              break;
+            }
+            k = prev;
+          }
+          if (k == col) {
+            found = (int)slot;
+            break;
+          }
+          slot = (slot + 1) & (unsigned)(cap - 1);
+        }
+        if (found < 0) {
+          *s_flag = 1;
+        } else {
+          unsigned m = peers;
+          T acc = fresh ? sv[__ffs(m) - 1] : hv[found] + sv[__ffs(m) - 1];
+          m &= m - 1;
+          while (m) {
+            acc = acc + sv[__ffs(m) - 1];
+            m &= m - 1;
+          }
+          hv[found] = acc;
+        }
+      }
+      __syncwarp();
+    }
+  }
+  return *s_flag == 0;
+}
+
 template <class T>
 __global__ void hash_warp_kernel(EscArgs<T> a, const int32_t* toff, int32_t* tci, T* tv, int32_t* counts,
                                  int32_t* over, int32_t* nover) {
   __shared__ int32_t hk[kHashWarps][kHashWarpCap];
   __shared__ T hv[kHashWarps][kHashWarpCap];
   __shared__ unsigned long long lst[kHashWarps][kHashWarpCap];
+  __shared__ T sv[kHashWarps][32];
   __shared__ int s_flag[kHashWarps];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int i = blockIdx.x * kHashWarps + w; i < a.n; i += gridDim.x * kHashWarps) {
-    bool ok = hash_row_accumulate<T>(a, i, hk[w], hv[w], kHashWarpCap, lane, 32, &s_flag[w], WarpSync());
+    bool ok = hash_row_accumulate_matched<T>(a, i, hk[w], hv[w], sv[w], kHashWarpCap, lane, &s_flag[w]);
     if (!ok) {
       if (lane == 0) {
         over[atomicAdd(nover, 1)] = i;
@@ -1375,35 +1546,17 @@ __global__ void partition_rows_kernel(int npart, const int32_t* part_idx, const 
   if (p < npart) rows[p] = agg_idx[part_idx[p + 1]] - agg_idx[part_idx[p]];
 }
 
+__global__ void row_lengths_kernel(int n, const int32_t* rp, int32_t* len) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) len[i] = rp[i + 1] - rp[i];
+}
+
 // In-partition entries per partition (the shared-memory footprint of the smoother).
 __global__ void partition_entries_kernel(int npart, const int32_t* part_idx, const int32_t* agg_idx,
                                          const int32_t* irp, int32_t* ent) {
   int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p < npart) ent[p] = irp[agg_idx[part_idx[p + 1]]] - irp[agg_idx[part_idx[p]]];
 }
-
-// Opt-in setup phase timing (environment FEMGPU_PROFILE set): synchronizes between
-// phases and prints the host wall time of each to stderr.
-struct PhaseTimer {
-  bool on;
-  cudaStream_t s;
-  int level;
-  std::chrono::steady_clock::time_point t0;
-  PhaseTimer(cudaStream_t st, int lvl) : on(getenv("FEMGPU_PROFILE") != nullptr), s(st), level(lvl) {
-    if (on) {
-      cudaStreamSynchronize(s);
-      t0 = std::chrono::steady_clock::now();
-    }
-  }
-  void mark(const char* what) {
-    if (!on) return;
-    cudaStreamSynchronize(s);
-    auto t = std::chrono::steady_clock::now();
-    fprintf(stderr, "[femgpu setup] level %d %-10s %8.3f ms\n", level, what,
-            std::chrono::duration<double, std::milli>(t - t0).count());
-    t0 = t;
-  }
-};
 
 template <class T>
 void build_levels(Ctx& c, Hierarchy<T>& H) {
@@ -1499,6 +1652,9 @@ void build_levels(Ctx& c, Hierarchy<T>& H) {
       FG_LAUNCH(partition_entries_kernel, grid_for(L.npart, 256), 256, 0, s, L.npart, L.part_idx.p, L.agg_idx.p,
                 L.Ain.rp.p, pent.p);
       L.max_part_entries = reduce_max(pent.p, L.npart, s);
+      DBuf<int32_t> rlen(N + 1, s);
+      FG_LAUNCH(row_lengths_kernel, grid_for(N, 256), 256, 0, s, N, L.Ain.rp.p, rlen.p);
+      L.max_in_row = reduce_max(rlen.p, N, s);
     }
     pt.mark("split");
     // prolongator and restrictor

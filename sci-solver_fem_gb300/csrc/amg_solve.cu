@@ -110,17 +110,23 @@ size_t part_smem_bytes(int mcap, int ecap) {
   return (size_t)mcap * 5 * sizeof(T) + (size_t)ecap * sizeof(T) + (size_t)(mcap + 1) * 4 + (size_t)ecap * 2 + 16;
 }
 
-// Sum over row t's in-partition entries in ascending column order, products rounded
-// separately (the reference adds them with shared-memory atomics in any order).
-template <class T, bool STAGED>
-__device__ __forceinline__ T part_row_sum(const PartSmem<T>& P, int t, const int32_t* __restrict__ ici,
-                                          const T* __restrict__ iv, int es, int rs) {
+// Sum over row t's in-partition entries with S lanes per row: lane j adds entries
+// j, j+S, ... in order (products rounded separately; the reference adds them with
+// shared-memory atomics in any order), then an xor butterfly combines the lanes.
+// Every lane of the warp must call it (the butterfly shuffles the whole warp).
+template <class T, bool STAGED, int S>
+__device__ __forceinline__ T part_row_sum(const PartSmem<T>& P, int t, bool live, int j,
+                                          const int32_t* __restrict__ ici, const T* __restrict__ iv, int es, int rs) {
   T s = 0;
-  const int q0 = P.srp[t], q1 = P.srp[t + 1];
-  for (int q = q0; q < q1; q++) {
-    if (STAGED) s = s + P.sval[q] * P.sx[P.scol[q]];
-    else s = s + iv[es + q] * P.sx[ici[es + q] - rs];
+  if (live) {
+    const int q0 = P.srp[t], q1 = P.srp[t + 1];
+    for (int q = q0 + j; q < q1; q += S) {
+      if (STAGED) s = s + P.sval[q] * P.sx[P.scol[q]];
+      else s = s + iv[es + q] * P.sx[ici[es + q] - rs];
+    }
   }
+#pragma unroll
+  for (int off = S >> 1; off > 0; off >>= 1) s = s + __shfl_xor_sync(0xffffffffu, s, off, S);
   return s;
 }
 
@@ -130,7 +136,7 @@ __device__ __forceinline__ T part_row_sum(const PartSmem<T>& P, int t, const int
 //   r = b - A_in x - d x are written;
 // POST == true (postRelaxSym_kernel, gauss_seidel.cu:3626-3736): b' = b - A_out x_in,
 //   `inner` sweeps from x_in, result written to x_out.
-template <class T, bool POST, bool STAGED>
+template <class T, bool POST, bool STAGED, int S>
 __global__ void __launch_bounds__(256) smooth_kernel(
     const int32_t* __restrict__ part_idx, const int32_t* __restrict__ agg_idx, const int32_t* __restrict__ irp,
     const int32_t* __restrict__ ici, const T* __restrict__ iv, const int32_t* __restrict__ orp,
@@ -166,10 +172,23 @@ __global__ void __launch_bounds__(256) smooth_kernel(
       P.scol[q] = (uint16_t)(ici[es + q] - rs);
     }
   __syncthreads();
+  const int j = threadIdx.x & (S - 1), per = blockDim.x / S;
   for (int it = 0; it < inner; it++) {
-    for (int t = threadIdx.x; t < m; t += blockDim.x) P.sax[t] = part_row_sum<T, STAGED>(P, t, ici, iv, es, rs);
+    for (int base = 0; base < m; base += per) {
+      const int t = base + threadIdx.x / S;
+      const T v = part_row_sum<T, STAGED, S>(P, t, t < m, j, ici, iv, es, rs);
+      if (j == 0 && t < m) P.sax[t] = v;
+    }
     __syncthreads();
     for (int t = threadIdx.x; t < m; t += blockDim.x) P.sx[t] = relax(P.sx[t], P.sb[t], P.sax[t], P.sd[t], P.sdi[t], w);
+    __syncthreads();
+  }
+  if (!POST) {
+    for (int base = 0; base < m; base += per) {
+      const int t = base + threadIdx.x / S;
+      const T v = part_row_sum<T, STAGED, S>(P, t, t < m, j, ici, iv, es, rs);
+      if (j == 0 && t < m) P.sax[t] = v;
+    }
     __syncthreads();
   }
   for (int t = threadIdx.x; t < m; t += blockDim.x) {
@@ -177,8 +196,77 @@ __global__ void __launch_bounds__(256) smooth_kernel(
     const T xv = P.sx[t];
     x_out[row] = xv;
     if (!POST) {
-      T u = P.sb[t] - part_row_sum<T, STAGED>(P, t, ici, iv, es, rs);
+      T u = P.sb[t] - P.sax[t];
       r_out[row] = u - P.sd[t] * xv;
+    }
+  }
+}
+
+
+// Register-resident variant for partitions of at most 1024 rows whose in-partition
+// rows have at most K entries: one thread per row keeps its entries (value, local
+// column) in registers across the sweeps, only x lives in shared memory.  Same
+// arithmetic and order as smooth_kernel.
+template <class T, bool POST, int K>
+__global__ void __launch_bounds__(1024) smooth_reg_kernel(
+    const int32_t* __restrict__ part_idx, const int32_t* __restrict__ agg_idx, const int32_t* __restrict__ irp,
+    const int32_t* __restrict__ ici, const T* __restrict__ iv, const int32_t* __restrict__ orp,
+    const int32_t* __restrict__ oci, const T* __restrict__ ov, const T* __restrict__ diag,
+    const T* __restrict__ dinv, const T* __restrict__ b, T w, int inner, const T* __restrict__ x_in,
+    T* __restrict__ x_out, T* __restrict__ r_out) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  T* sx = reinterpret_cast<T*>(sm);
+  const int rs = agg_idx[part_idx[blockIdx.x]], re = agg_idx[part_idx[blockIdx.x + 1]];
+  const int t = threadIdx.x;
+  const bool live = t < re - rs;
+  const int row = rs + t;
+  T val[K];
+  int col[K];
+  int len = 0;
+  T d = (T)1, di = (T)1, bb = (T)0, x = (T)0;
+  if (live) {
+    const int e0 = irp[row];
+    len = irp[row + 1] - e0;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      val[k] = k < len ? iv[e0 + k] : (T)0;
+      col[k] = k < len ? ici[e0 + k] - rs : 0;
+    }
+    d = diag[row];
+    di = dinv[row];
+    if (POST) {
+      T acc = b[row];
+      for (int e = orp[row]; e < orp[row + 1]; e++) acc = acc + (-ov[e]) * x_in[oci[e]];
+      bb = acc;
+      x = x_in[row];
+    } else {
+      bb = b[row];
+      x = (w * bb) * di;
+    }
+    sx[t] = x;
+  }
+  __syncthreads();
+  for (int it = 0; it < inner; it++) {
+    T sax = 0;
+#pragma unroll
+    for (int k = 0; k < K; k++)
+      if (k < len) sax = sax + val[k] * sx[col[k]];
+    __syncthreads();
+    if (live) {
+      x = relax(x, bb, sax, d, di, w);
+      sx[t] = x;
+    }
+    __syncthreads();
+  }
+  if (live) {
+    x_out[row] = x;
+    if (!POST) {
+      T sax = 0;
+#pragma unroll
+      for (int k = 0; k < K; k++)
+        if (k < len) sax = sax + val[k] * sx[col[k]];
+      T u = bb - sax;
+      r_out[row] = u - d * x;
     }
   }
 }
@@ -211,14 +299,18 @@ __global__ void spmv_lanes_kernel(int n, const int32_t* __restrict__ rp, const i
   if (live && j == 0) y[g] = accumulate ? y[g] + s : s;
 }
 
-// Coarsest level: x = A^-1 b with the explicit FP64 inverse.
+// Coarsest level: x = A^-1 b with the explicit FP64 inverse, one warp per row: lane j
+// accumulates columns j, j+32, ... with fma, then an xor butterfly (the oracle uses
+// the same order).
 template <class T>
 __global__ void coarse_solve_kernel(int n, const double* __restrict__ inv, const T* __restrict__ b, T* __restrict__ x) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   double s = 0.0;
-  for (int j = 0; j < n; j++) s = fma(inv[(int64_t)i * n + j], (double)b[j], s);
-  x[i] = (T)s;
+  if (i < n)
+    for (int j = lane; j < n; j += 32) s = fma(inv[(int64_t)i * n + j], (double)b[j], s);
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) s = s + __shfl_xor_sync(0xffffffffu, s, off);
+  if (i < n && lane == 0) x[i] = (T)s;
 }
 
 // ---- FP64 PCG kernels -----------------------------------------------------------------
@@ -246,6 +338,7 @@ __global__ void spmv_kernel(int n, const int32_t* __restrict__ rp, const int32_t
   for (int e = rp[i]; e < rp[i + 1]; e++) s = fma(v[e], x[ci[e]], s);
   y[i] = s;
 }
+
 
 // partial dot(a, b) (and dot(a, c) when c != nullptr into partial2)
 __global__ void dot_kernel(int n, const double* __restrict__ a, const double* __restrict__ b,
@@ -379,29 +472,45 @@ size_t smooth_smem(const Level<T>& L) {
   return part_smem_bytes<T>(L.max_part_rows, staged(L) ? L.max_part_entries : 0);
 }
 
-template <class T>
-void set_smem_attrs(const Level<T>& L) {
-  const int bytes = (int)smooth_smem(L);
-  if (bytes <= 48 * 1024) return;
-  FG_CUDA(cudaFuncSetAttribute(smooth_kernel<T, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-  FG_CUDA(cudaFuncSetAttribute(smooth_kernel<T, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-  FG_CUDA(cudaFuncSetAttribute(smooth_kernel<T, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-  FG_CUDA(cudaFuncSetAttribute(smooth_kernel<T, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-}
+
+constexpr int kRegRow = 16;
 
 template <class T>
 void smooth(Ctx& c, Level<T>& L, bool post, const T* b, const T* xin, T* xout, T* rout) {
   cudaStream_t s = c.stream;
   const T w = (T)c.cfg.smootherWeight;
   const int inner = post ? c.cfg.postInnerIters : c.cfg.preInnerIters;
+  if (L.max_in_row <= kRegRow && L.max_part_rows <= 1024) {
+    const int thr = ((L.max_part_rows + 31) / 32) * 32;
+    auto k = post ? smooth_reg_kernel<T, true, kRegRow> : smooth_reg_kernel<T, false, kRegRow>;
+    FG_LAUNCH(k, L.npart, thr < 32 ? 32 : thr, (size_t)thr * sizeof(T), s, L.part_idx.p, L.agg_idx.p, L.Ain.rp.p,
+              L.Ain.ci.p, L.Ain.v.p, L.Aout.rp.p, L.Aout.ci.p, L.Aout.v.p, L.diag.p, L.dinv.p, b, w, inner, xin, xout,
+              rout);
+    return;
+  }
   const size_t sm = smooth_smem(L);
   const bool st = staged(L);
-  auto k = post ? (st ? smooth_kernel<T, true, true> : smooth_kernel<T, true, false>)
-                : (st ? smooth_kernel<T, false, true> : smooth_kernel<T, false, false>);
+  const int S = lanes_for_rows(L.Ain.nnz, L.n);
+  using KFn = void (*)(const int32_t*, const int32_t*, const int32_t*, const int32_t*, const T*, const int32_t*,
+                       const int32_t*, const T*, const T*, const T*, const T*, T, int, const T*, T*, T*, int, int);
+  KFn k;
+#define FG_SMOOTH_PICK(SS)                                                                  \
+  k = post ? (st ? smooth_kernel<T, true, true, SS> : smooth_kernel<T, true, false, SS>)    \
+           : (st ? smooth_kernel<T, false, true, SS> : smooth_kernel<T, false, false, SS>)
+  switch (S) {
+    case 1: FG_SMOOTH_PICK(1); break;
+    case 2: FG_SMOOTH_PICK(2); break;
+    case 4: FG_SMOOTH_PICK(4); break;
+    case 8: FG_SMOOTH_PICK(8); break;
+    case 16: FG_SMOOTH_PICK(16); break;
+    default: FG_SMOOTH_PICK(32); break;
+  }
+#undef FG_SMOOTH_PICK
   // the limit is a per-function attribute shared by every handle: set it per launch
   if (sm > 48 * 1024) FG_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   FG_LAUNCH(k, L.npart, 256, sm, s, L.part_idx.p, L.agg_idx.p, L.Ain.rp.p, L.Ain.ci.p, L.Ain.v.p, L.Aout.rp.p,
-            L.Aout.ci.p, L.Aout.v.p, L.diag.p, L.dinv.p, b, w, inner, xin, xout, rout, L.max_part_rows, L.max_part_entries);
+            L.Aout.ci.p, L.Aout.v.p, L.diag.p, L.dinv.p, b, w, inner, xin, xout, rout, L.max_part_rows,
+            L.max_part_entries);
 }
 
 // b (level order for l > 0, already permuted for l == 0) -> x (same ordering).
@@ -411,7 +520,7 @@ void vcycle(Ctx& c, Hierarchy<T>& H, int l, const T* b_in, T* x_out) {
   Level<T>& L = *H.L[l];
   const int n = L.A.n;
   if (L.coarsest) {
-    FG_LAUNCH(coarse_solve_kernel<T>, grid_for(n, 128), 128, 0, s, n, L.Ainv.p, b_in, x_out);
+    FG_LAUNCH(coarse_solve_kernel<T>, grid_for((int64_t)n * 32, 256), 256, 0, s, n, L.Ainv.p, b_in, x_out);
     return;
   }
   const T* b = b_in;
@@ -563,11 +672,6 @@ bool capture_iteration(Ctx& c, int n, int flexible) {
   return true;
 }
 
-template <class T>
-void set_all_smem_attrs(Hierarchy<T>& H) {
-  for (auto& L : H.L)
-    if (!L->coarsest) set_smem_attrs(*L);
-}
 
 }  // namespace
 
@@ -576,8 +680,6 @@ SolveResult amg_solve_device(Ctx& c, const double* d_b, double* d_x) {
   const int n = c.A.n;
   cudaStream_t s = c.stream;
   ensure_work(c, n);
-  if (c.cfg.precision == 1) set_all_smem_attrs(static_cast<Hierarchy<double>&>(*c.H));
-  else set_all_smem_attrs(static_cast<Hierarchy<float>&>(*c.H));
   SolveResult res;
   double* part = c.red.p;
   double* sc = c.red.p + 2 * kRedBlocks;
@@ -645,6 +747,100 @@ SolveResult amg_solve_device(Ctx& c, const double* d_b, double* d_x) {
   res.iterations = it;
   res.relres = nr / bnorm;
   return res;
+}
+
+namespace {
+
+template <class T>
+__global__ void fill_value_kernel(int64_t n, T* a, T v) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) a[i] = v;
+}
+
+template <class T>
+void profile_level0(Ctx& c, Hierarchy<T>& H, int which, int reps, double* ms, double* bytes) {
+  cudaStream_t s = c.stream;
+  Level<T>& L = *H.L[0];
+  FG_REQUIRE(!L.coarsest, FEMGPU_ERR_INVALID, "level 0 is the coarsest level: no smoother to time");
+  const int n = L.n;
+  const double ts = sizeof(T);
+  // well-defined inputs
+  FG_LAUNCH(fill_value_kernel<T>, grid_for(n, 256), 256, 0, s, (int64_t)n, L.b.p, (T)1);
+  FG_LAUNCH(fill_value_kernel<T>, grid_for(n, 256), 256, 0, s, (int64_t)n, L.x.p, (T)0.5);
+  FG_LAUNCH(fill_value_kernel<T>, grid_for(n, 256), 256, 0, s, (int64_t)n, L.r.p, (T)0.25);
+  FG_LAUNCH(fill_value_kernel<T>, grid_for(L.nagg, 256), 256, 0, s, (int64_t)L.nagg, L.t.p, (T)0.125);
+  auto run = [&]() {
+    switch (which) {
+      case 1: smooth<T>(c, L, false, L.b.p, nullptr, L.x.p, L.r.p); break;
+      case 2: smooth<T>(c, L, true, L.b.p, L.x.p, L.xo.p, nullptr); break;
+      case 3: spmv_lanes(L.R, L.r.p, L.t.p, 0, s); break;
+      default: spmv_lanes(L.P, L.t.p, L.xo.p, 1, s); break;
+    }
+  };
+  switch (which) {
+    case 1:
+      *bytes = L.Ain.nnz * (ts + 4) + 4.0 * (n + 1) + 3 * ts * n + 2 * ts * n;
+      break;
+    case 2:
+      *bytes = (L.Ain.nnz + L.Aout.nnz) * (ts + 4) + 8.0 * (n + 1) + 4 * ts * n + ts * n;
+      break;
+    case 3:
+      *bytes = L.R.nnz * (ts + 4) + 4.0 * (L.nagg + 1) + ts * n + ts * L.nagg;
+      break;
+    default:
+      *bytes = L.P.nnz * (ts + 4) + 4.0 * (n + 1) + ts * L.nagg + 2 * ts * n;
+      break;
+  }
+  for (int i = 0; i < 3; i++) run();
+  cudaEvent_t e0, e1;
+  FG_CUDA(cudaEventCreate(&e0));
+  FG_CUDA(cudaEventCreate(&e1));
+  FG_CUDA(cudaEventRecord(e0, s));
+  for (int i = 0; i < reps; i++) run();
+  FG_CUDA(cudaEventRecord(e1, s));
+  FG_CUDA(cudaEventSynchronize(e1));
+  float t = 0;
+  FG_CUDA(cudaEventElapsedTime(&t, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms = t / reps;
+}
+
+}  // namespace
+
+// Times one hot kernel with CUDA events on the handle's stream (after 3 untimed
+// launches) and reports its algorithmic bytes: 0 = the outer PCG's FP64 SpMV
+// (CSR, fused dot), 1 = level-0 pre-smoother, 2 = level-0 post-smoother relax,
+// 3 = level-0 restriction R r, 4 = level-0 prolongation x += P xc.
+void profile_kernel(Ctx& c, int which, int reps, double* ms, double* bytes) {
+  FG_REQUIRE(c.has_hierarchy, FEMGPU_ERR_NOT_READY, "call femgpu_setup first");
+  FG_REQUIRE(reps > 0 && which >= 0 && which <= 4, FEMGPU_ERR_INVALID, "bad kernel selector");
+  cudaStream_t s = c.stream;
+  if (which == 0) {
+    const int n = c.A.n;
+    ensure_work(c, n);
+    FG_LAUNCH(fill_value_kernel<double>, grid_for(n, 256), 256, 0, s, (int64_t)n, c.vp.p, 1.0);
+    auto run = [&]() {
+      FG_LAUNCH(spmv_dot_kernel, kRedBlocks, kRedThreads, 0, s, n, c.A0p.rp.p, c.A0p.ci.p, c.A0p.v.p, c.vp.p, c.vy.p,
+                c.red.p);
+    };
+    for (int i = 0; i < 3; i++) run();
+    cudaEvent_t e0, e1;
+    FG_CUDA(cudaEventCreate(&e0));
+    FG_CUDA(cudaEventCreate(&e1));
+    FG_CUDA(cudaEventRecord(e0, s));
+    for (int i = 0; i < reps; i++) run();
+    FG_CUDA(cudaEventRecord(e1, s));
+    FG_CUDA(cudaEventSynchronize(e1));
+    float t = 0;
+    FG_CUDA(cudaEventElapsedTime(&t, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms = t / reps;
+    *bytes = 12.0 * c.A0p.nnz + 4.0 * (n + 1) + 8.0 * n + 8.0 * n;
+    return;
+  }
+  if (c.cfg.precision == 1) profile_level0(c, static_cast<Hierarchy<double>&>(*c.H), which, reps, ms, bytes);
+  else profile_level0(c, static_cast<Hierarchy<float>&>(*c.H), which, reps, ms, bytes);
 }
 
 }  // namespace femgpu

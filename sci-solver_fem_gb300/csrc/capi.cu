@@ -434,6 +434,11 @@ femgpu_status femgpu_vcycle(femgpu_handle h, const double* r, double* z) {
   });
 }
 
+femgpu_status femgpu_profile_kernel(femgpu_handle h, int which, int reps, double* avg_ms, double* bytes) {
+  if (!h || !avg_ms || !bytes) return FEMGPU_ERR_INVALID;
+  return guard(h, [&] { profile_kernel(*h, which, reps, avg_ms, bytes); });
+}
+
 femgpu_status femgpu_kernel_launches(femgpu_handle h, int64_t* count) {
   (void)h;
   if (!count) return FEMGPU_ERR_INVALID;

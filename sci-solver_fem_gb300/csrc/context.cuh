@@ -52,6 +52,7 @@ struct Level {
   DBuf<T> diag, dinv;  // diagonal of Ap and its reciprocal
   int max_part_rows = 0;
   int max_part_entries = 0;  // in-partition off-diagonal entries of the largest partition
+  int max_in_row = 0;        // longest in-partition row
   // coarsest: explicit inverse, row-major n x n
   DBuf<double> Ainv;
   // work vectors (level numbering / permuted numbering)
@@ -122,5 +123,6 @@ struct SolveResult {
 SolveResult amg_solve_device(Ctx& c, const double* d_b, double* d_x);
 void amg_vcycle_device(Ctx& c, const double* d_r, double* d_z);
 void spmv_original(Ctx& c, const double* d_x, double* d_y);
+void profile_kernel(Ctx& c, int which, int reps, double* ms, double* bytes);
 
 }  // namespace femgpu

@@ -25,6 +25,7 @@ EXPORTS = [
     "femgpu_set_mesh", "femgpu_assemble", "femgpu_load_vector", "femgpu_set_dirichlet", "femgpu_set_matrix_csr",
     "femgpu_setup", "femgpu_solve", "femgpu_solve_device", "femgpu_spmv_device", "femgpu_get_matrix",
     "femgpu_num_levels", "femgpu_get_level_info", "femgpu_level_get", "femgpu_vcycle", "femgpu_kernel_launches",
+    "femgpu_profile_kernel",
     "femgpu_read_tetgen", "femgpu_read_ply", "femgpu_read_mat_sparse", "femgpu_read_mat_array",
     "femgpu_write_mat_array", "femgpu_write_vtk",
 ]
@@ -100,6 +101,7 @@ def lib():
     L.femgpu_level_get.argtypes = [_vp, C.c_int] + [_vp] * 9
     L.femgpu_vcycle.argtypes = [_vp, _f64p, _f64p]
     L.femgpu_kernel_launches.argtypes = [_vp, _pi64]
+    L.femgpu_profile_kernel.argtypes = [_vp, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.femgpu_read_tetgen.argtypes = [C.c_char_p, C.c_char_p, _pi64, _pi64, _vp, _vp, _vp]
     L.femgpu_read_ply.argtypes = [C.c_char_p, _pi64, _pi64, _vp, _vp]
     L.femgpu_read_mat_sparse.argtypes = [C.c_char_p, _pi64, _pi64, _pi64, _vp, _vp, _vp]
@@ -256,6 +258,14 @@ class Solver:
             _check(status, self.h)
         return dict(status=status, iterations=st.iterations, relres=st.relative_residual,
                     setup_ms=st.setup_ms, solve_ms=st.solve_ms, levels=st.num_levels)
+
+    KERNELS = {0: "spmv_dot_kernel (FP64 CSR outer SpMV + dot)", 1: "smooth pre (level 0)", 2: "smooth post (level 0)",
+               3: "spmv_lanes R (level 0)", 4: "spmv_lanes P (level 0)"}
+
+    def profile_kernel(self, which: int, reps: int = 20):
+        ms, nb = C.c_double(), C.c_double()
+        _check(lib().femgpu_profile_kernel(self.h, which, reps, C.byref(ms), C.byref(nb)), self.h)
+        return ms.value, nb.value
 
     def spmv_device(self, x_ptr: int, y_ptr: int):
         _check(lib().femgpu_spmv_device(self.h, _vp(x_ptr), _vp(y_ptr)), self.h)
