@@ -1133,12 +1133,14 @@ int setup_levels(orc_amg* h, std::vector<Level<T>>& L, const Csr<double>& A, con
     split_partitions(lv);
     {
       /* the device keeps rows of <= 16 in-partition entries in registers (one lane per
-       * row) when partitions have <= 1024 rows, else sums rows with S lanes */
+       * row) when partitions have <= 512 rows, else sums rows with S lanes */
       int max_row = 0, max_part = 0;
       for (int i = 0; i < N; i++) max_row = std::max(max_row, lv.Ain.rp[i + 1] - lv.Ain.rp[i]);
       for (size_t q = 0; q + 1 < lv.partIdx.size(); q++)
         max_part = std::max(max_part, lv.aggIdx[lv.partIdx[q + 1]] - lv.aggIdx[lv.partIdx[q]]);
-      lv.smooth_lanes = (max_row <= 16 && max_part <= 1024) ? 1 : lanes_for_rows(lv.Ain.nnz(), N);
+      int sl = 1; /* 1024-thread CTAs: as many lanes per row as the largest partition allows */
+      while (sl < 32 && (int64_t)(sl * 2) * max_part <= 1024) sl <<= 1;
+      lv.smooth_lanes = (max_row <= 16 && max_part <= 512) ? 1 : sl;
     }
     lv.P = build_prolongator(lv.Ap, lv.diag, lv.aggOf, nagg, c.pro_omega);
     lv.R = transpose(lv.P);

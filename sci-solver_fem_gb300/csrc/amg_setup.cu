@@ -1724,6 +1724,7 @@ void build_levels(Ctx& c, Hierarchy<T>& H) {
     L.r.alloc(N, s);
     L.xo.alloc(N, s);
     L.t.alloc(N, s);
+    L.bp.alloc(N, s);
     H.L.push_back(std::move(nx));
     num_levels++;
   }

@@ -137,7 +137,7 @@ __device__ __forceinline__ T part_row_sum(const PartSmem<T>& P, int t, bool live
 // POST == true (postRelaxSym_kernel, gauss_seidel.cu:3626-3736): b' = b - A_out x_in,
 //   `inner` sweeps from x_in, result written to x_out.
 template <class T, bool POST, bool STAGED, int S>
-__global__ void __launch_bounds__(256) smooth_kernel(
+__global__ void __launch_bounds__(1024) smooth_kernel(
     const int32_t* __restrict__ part_idx, const int32_t* __restrict__ agg_idx, const int32_t* __restrict__ irp,
     const int32_t* __restrict__ ici, const T* __restrict__ iv, const int32_t* __restrict__ orp,
     const int32_t* __restrict__ oci, const T* __restrict__ ov, const T* __restrict__ diag,
@@ -156,7 +156,8 @@ __global__ void __launch_bounds__(256) smooth_kernel(
     P.srp[t] = irp[row] - es;
     if (POST) {
       T acc = b[row];
-      for (int e = orp[row]; e < orp[row + 1]; e++) acc = acc + (-ov[e]) * x_in[oci[e]];
+      if (orp)
+        for (int e = orp[row]; e < orp[row + 1]; e++) acc = acc + (-ov[e]) * x_in[oci[e]];
       P.sb[t] = acc;
       P.sx[t] = x_in[row];
     } else {
@@ -208,7 +209,7 @@ __global__ void __launch_bounds__(256) smooth_kernel(
 // column) in registers across the sweeps, only x lives in shared memory.  Same
 // arithmetic and order as smooth_kernel.
 template <class T, bool POST, int K>
-__global__ void __launch_bounds__(1024) smooth_reg_kernel(
+__global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
     const int32_t* __restrict__ part_idx, const int32_t* __restrict__ agg_idx, const int32_t* __restrict__ irp,
     const int32_t* __restrict__ ici, const T* __restrict__ iv, const int32_t* __restrict__ orp,
     const int32_t* __restrict__ oci, const T* __restrict__ ov, const T* __restrict__ diag,
@@ -221,22 +222,26 @@ __global__ void __launch_bounds__(1024) smooth_reg_kernel(
   const bool live = t < re - rs;
   const int row = rs + t;
   T val[K];
-  int col[K];
+  uint32_t colp[K / 2];  // two 16-bit local columns per register
   int len = 0;
   T d = (T)1, di = (T)1, bb = (T)0, x = (T)0;
   if (live) {
     const int e0 = irp[row];
     len = irp[row + 1] - e0;
 #pragma unroll
-    for (int k = 0; k < K; k++) {
+    for (int k = 0; k < K; k += 2) {
       val[k] = k < len ? iv[e0 + k] : (T)0;
-      col[k] = k < len ? ici[e0 + k] - rs : 0;
+      val[k + 1] = k + 1 < len ? iv[e0 + k + 1] : (T)0;
+      const uint32_t c0 = k < len ? (uint32_t)(ici[e0 + k] - rs) : 0u;
+      const uint32_t c1 = k + 1 < len ? (uint32_t)(ici[e0 + k + 1] - rs) : 0u;
+      colp[k >> 1] = c0 | (c1 << 16);
     }
     d = diag[row];
     di = dinv[row];
     if (POST) {
       T acc = b[row];
-      for (int e = orp[row]; e < orp[row + 1]; e++) acc = acc + (-ov[e]) * x_in[oci[e]];
+      if (orp)
+        for (int e = orp[row]; e < orp[row + 1]; e++) acc = acc + (-ov[e]) * x_in[oci[e]];
       bb = acc;
       x = x_in[row];
     } else {
@@ -250,7 +255,7 @@ __global__ void __launch_bounds__(1024) smooth_reg_kernel(
     T sax = 0;
 #pragma unroll
     for (int k = 0; k < K; k++)
-      if (k < len) sax = sax + val[k] * sx[col[k]];
+      if (k < len) sax = sax + val[k] * sx[(colp[k >> 1] >> ((k & 1) * 16)) & 0xffffu];
     __syncthreads();
     if (live) {
       x = relax(x, bb, sax, d, di, w);
@@ -264,7 +269,7 @@ __global__ void __launch_bounds__(1024) smooth_reg_kernel(
       T sax = 0;
 #pragma unroll
       for (int k = 0; k < K; k++)
-        if (k < len) sax = sax + val[k] * sx[col[k]];
+        if (k < len) sax = sax + val[k] * sx[(colp[k >> 1] >> ((k & 1) * 16)) & 0xffffu];
       T u = bb - sax;
       r_out[row] = u - d * x;
     }
@@ -437,7 +442,7 @@ __global__ void perm_vec_out_kernel(int n, const int32_t* perm, const double* in
 }
 
 // ---- V-cycle driver ------------------------------------------------------------------
-constexpr size_t kStageLimit = 160 * 1024;  // staged smoother: keep >= 1 CTA per SM with room
+constexpr size_t kStageLimit = 200 * 1024;  // staged smoother: one 1024-thread CTA per SM
 
 // Lanes per row for the R/P products: the same rule in the CPU oracle.
 inline int lanes_for_rows(int64_t nnz, int n) {
@@ -475,22 +480,51 @@ size_t smooth_smem(const Level<T>& L) {
 
 constexpr int kRegRow = 16;
 
+// Lanes per row of the shared-memory smoother: 1024-thread CTAs, as many lanes per
+// row as the largest partition allows (the CPU oracle uses the same rule).
+inline int smem_lanes(int max_part_rows) {
+  int s = 1;
+  while (s < 32 && (int64_t)(s * 2) * max_part_rows <= 1024) s <<= 1;
+  return s;
+}
+
+// Post-smoother right-hand side b' = b - A_out x (the first loop of
+// postRelaxSym_kernel, gauss_seidel.cu:3676-3684), one thread per row.
+template <class T>
+__global__ void aout_rhs_kernel(int n, const int32_t* __restrict__ orp, const int32_t* __restrict__ oci,
+                                const T* __restrict__ ov, const T* __restrict__ b, const T* __restrict__ x,
+                                T* __restrict__ bp) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  T acc = b[i];
+  for (int e = orp[i]; e < orp[i + 1]; e++) acc = acc + (-ov[e]) * x[oci[e]];
+  bp[i] = acc;
+}
+
+// Post relaxes take b' from aout_rhs_kernel (orp == nullptr inside the smoother).
 template <class T>
 void smooth(Ctx& c, Level<T>& L, bool post, const T* b, const T* xin, T* xout, T* rout) {
   cudaStream_t s = c.stream;
+  const int32_t* aorp = L.Aout.rp.p;
+  if (post) {
+    FG_LAUNCH(aout_rhs_kernel<T>, grid_for(L.n, 256), 256, 0, s, L.n, L.Aout.rp.p, L.Aout.ci.p, L.Aout.v.p, b, xin,
+              L.bp.p);
+    b = L.bp.p;
+    aorp = nullptr;
+  }
   const T w = (T)c.cfg.smootherWeight;
   const int inner = post ? c.cfg.postInnerIters : c.cfg.preInnerIters;
-  if (L.max_in_row <= kRegRow && L.max_part_rows <= 1024) {
+  if (L.max_in_row <= kRegRow && L.max_part_rows <= 512) {
     const int thr = ((L.max_part_rows + 31) / 32) * 32;
     auto k = post ? smooth_reg_kernel<T, true, kRegRow> : smooth_reg_kernel<T, false, kRegRow>;
     FG_LAUNCH(k, L.npart, thr < 32 ? 32 : thr, (size_t)thr * sizeof(T), s, L.part_idx.p, L.agg_idx.p, L.Ain.rp.p,
-              L.Ain.ci.p, L.Ain.v.p, L.Aout.rp.p, L.Aout.ci.p, L.Aout.v.p, L.diag.p, L.dinv.p, b, w, inner, xin, xout,
+              L.Ain.ci.p, L.Ain.v.p, aorp, L.Aout.ci.p, L.Aout.v.p, L.diag.p, L.dinv.p, b, w, inner, xin, xout,
               rout);
     return;
   }
   const size_t sm = smooth_smem(L);
   const bool st = staged(L);
-  const int S = lanes_for_rows(L.Ain.nnz, L.n);
+  const int S = smem_lanes(L.max_part_rows);
   using KFn = void (*)(const int32_t*, const int32_t*, const int32_t*, const int32_t*, const T*, const int32_t*,
                        const int32_t*, const T*, const T*, const T*, const T*, T, int, const T*, T*, T*, int, int);
   KFn k;
@@ -508,7 +542,7 @@ void smooth(Ctx& c, Level<T>& L, bool post, const T* b, const T* xin, T* xout, T
 #undef FG_SMOOTH_PICK
   // the limit is a per-function attribute shared by every handle: set it per launch
   if (sm > 48 * 1024) FG_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  FG_LAUNCH(k, L.npart, 256, sm, s, L.part_idx.p, L.agg_idx.p, L.Ain.rp.p, L.Ain.ci.p, L.Ain.v.p, L.Aout.rp.p,
+  FG_LAUNCH(k, L.npart, 1024, sm, s, L.part_idx.p, L.agg_idx.p, L.Ain.rp.p, L.Ain.ci.p, L.Ain.v.p, aorp,
             L.Aout.ci.p, L.Aout.v.p, L.diag.p, L.dinv.p, b, w, inner, xin, xout, rout, L.max_part_rows,
             L.max_part_entries);
 }

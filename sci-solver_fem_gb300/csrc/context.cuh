@@ -56,7 +56,7 @@ struct Level {
   // coarsest: explicit inverse, row-major n x n
   DBuf<double> Ainv;
   // work vectors (level numbering / permuted numbering)
-  DBuf<T> b, x, r, xo, t;
+  DBuf<T> b, x, r, xo, t, bp;  // bp: post-smoother right-hand side
 };
 
 struct HierarchyBase {
