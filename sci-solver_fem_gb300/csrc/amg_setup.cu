@@ -16,6 +16,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cmath>
+#include <limits>
+#include <vector>
 
 #include "context.cuh"
 
@@ -1558,6 +1560,42 @@ __global__ void partition_entries_kernel(int npart, const int32_t* part_idx, con
   if (p < npart) ent[p] = irp[agg_idx[part_idx[p + 1]]] - irp[agg_idx[part_idx[p]]];
 }
 
+// First row and first in-partition entry of partitions 0..npart (npart = the end).
+__global__ void partition_starts_kernel(int npart, const int32_t* part_idx, const int32_t* agg_idx,
+                                        const int32_t* irp, int32_t* row0, int32_t* ent0) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p <= npart) {
+    const int r = agg_idx[part_idx[p]];
+    row0[p] = r;
+    ent0[p] = irp[r];
+  }
+}
+
+// Smoother work groups: consecutive partitions packed greedily into one CTA while
+// the group stays within `max_rows` rows and `max_ents` in-partition entries.
+template <class T>
+void build_smoother_groups(Ctx& c, Level<T>& L, int max_rows, int max_ents) {
+  cudaStream_t s = c.stream;
+  DBuf<int32_t> row0(L.npart + 1, s), ent0(L.npart + 1, s);
+  FG_LAUNCH(partition_starts_kernel, grid_for(L.npart + 1, 256), 256, 0, s, L.npart, L.part_idx.p, L.agg_idx.p,
+            L.Ain.rp.p, row0.p, ent0.p);
+  std::vector<int32_t> hr = row0.to_host(), he = ent0.to_host();
+  std::vector<int32_t> g{hr[0]};
+  int gp = 0, mx = 0;
+  for (int p = 1; p <= L.npart; p++) {
+    const bool last = p == L.npart;
+    if (last || hr[p + 1] - hr[gp] > max_rows || he[p + 1] - he[gp] > max_ents) {
+      g.push_back(hr[p]);
+      mx = std::max(mx, hr[p] - hr[gp]);
+      gp = p;
+    }
+  }
+  L.ngroups = (int)g.size() - 1;
+  L.max_group_rows = mx;
+  L.grows.alloc(g.size(), s);
+  L.grows.upload(g.data(), g.size());
+}
+
 template <class T>
 void build_levels(Ctx& c, Hierarchy<T>& H) {
   cudaStream_t s = c.stream;
@@ -1655,6 +1693,10 @@ void build_levels(Ctx& c, Hierarchy<T>& H) {
       DBuf<int32_t> rlen(N + 1, s);
       FG_LAUNCH(row_lengths_kernel, grid_for(N, 256), 256, 0, s, N, L.Ain.rp.p, rlen.p);
       L.max_in_row = reduce_max(rlen.p, N, s);
+      if (smoother_in_registers(L.max_in_row, L.max_part_rows))
+        build_smoother_groups(c, L, kRegGroupRows, std::numeric_limits<int>::max());
+      else
+        build_smoother_groups(c, L, L.max_part_rows, L.max_part_entries);
     }
     pt.mark("split");
     // prolongator and restrictor

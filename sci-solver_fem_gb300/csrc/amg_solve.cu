@@ -130,21 +130,25 @@ __device__ __forceinline__ T part_row_sum(const PartSmem<T>& P, int t, bool live
   return s;
 }
 
-// Partition-block Jacobi smoother, one CTA per partition.
+// Partition-block Jacobi smoother.  One CTA runs a group of consecutive partitions
+// (rows [grows[g], grows[g+1])): in-partition entries never leave their partition,
+// so a group of partitions is smoothed exactly like each partition on its own.
+// x is double-buffered in shared memory (one barrier per sweep).
 // POST == false (preRRSym_kernel + the in-partition part of the residual,
 //   gauss_seidel.cu:1278-1376): x0 = w b / d, `inner` sweeps, then x and
 //   r = b - A_in x - d x are written;
-// POST == true (postRelaxSym_kernel, gauss_seidel.cu:3626-3736): b' = b - A_out x_in,
-//   `inner` sweeps from x_in, result written to x_out.
+// POST == true (postRelaxSym_kernel, gauss_seidel.cu:3626-3736): b' = b - A_out x_in
+//   (precomputed by aout_rhs_kernel when orp == nullptr), `inner` sweeps from x_in,
+//   result written to x_out.
 template <class T, bool POST, bool STAGED, int S>
 __global__ void __launch_bounds__(1024) smooth_kernel(
-    const int32_t* __restrict__ part_idx, const int32_t* __restrict__ agg_idx, const int32_t* __restrict__ irp,
+    const int32_t* __restrict__ grows, const int32_t* __restrict__ irp,
     const int32_t* __restrict__ ici, const T* __restrict__ iv, const int32_t* __restrict__ orp,
     const int32_t* __restrict__ oci, const T* __restrict__ ov, const T* __restrict__ diag,
-    const T* __restrict__ dinv, const T* __restrict__ b, T w, int inner, const T* __restrict__ x_in, T* __restrict__ x_out, T* __restrict__ r_out, int mcap,
-    int ecap) {
+    const T* __restrict__ dinv, const T* __restrict__ b, T w, int inner, const T* __restrict__ x_in,
+    T* __restrict__ x_out, T* __restrict__ r_out, int mcap, int ecap) {
   extern __shared__ __align__(16) unsigned char sm[];
-  const int rs = agg_idx[part_idx[blockIdx.x]], re = agg_idx[part_idx[blockIdx.x + 1]];
+  const int rs = grows[blockIdx.x], re = grows[blockIdx.x + 1];
   const int m = re - rs;
   const int es = irp[rs], ne = irp[re] - es;
   PartSmem<T> P = carve<T>(sm, mcap, STAGED ? ecap : 0);
@@ -174,50 +178,52 @@ __global__ void __launch_bounds__(1024) smooth_kernel(
     }
   __syncthreads();
   const int j = threadIdx.x & (S - 1), per = blockDim.x / S;
+  T* cur = P.sx;
+  T* nxt = P.sax;
   for (int it = 0; it < inner; it++) {
+    P.sx = cur;
     for (int base = 0; base < m; base += per) {
       const int t = base + threadIdx.x / S;
       const T v = part_row_sum<T, STAGED, S>(P, t, t < m, j, ici, iv, es, rs);
-      if (j == 0 && t < m) P.sax[t] = v;
+      if (j == 0 && t < m) nxt[t] = relax(cur[t], P.sb[t], v, P.sd[t], P.sdi[t], w);
     }
     __syncthreads();
-    for (int t = threadIdx.x; t < m; t += blockDim.x) P.sx[t] = relax(P.sx[t], P.sb[t], P.sax[t], P.sd[t], P.sdi[t], w);
-    __syncthreads();
+    T* tmp = cur;
+    cur = nxt;
+    nxt = tmp;
   }
+  P.sx = cur;
   if (!POST) {
     for (int base = 0; base < m; base += per) {
       const int t = base + threadIdx.x / S;
       const T v = part_row_sum<T, STAGED, S>(P, t, t < m, j, ici, iv, es, rs);
-      if (j == 0 && t < m) P.sax[t] = v;
+      if (j == 0 && t < m) {
+        const T xv = cur[t];
+        x_out[rs + t] = xv;
+        T u = P.sb[t] - v;
+        r_out[rs + t] = u - P.sd[t] * xv;
+      }
     }
-    __syncthreads();
-  }
-  for (int t = threadIdx.x; t < m; t += blockDim.x) {
-    const int row = rs + t;
-    const T xv = P.sx[t];
-    x_out[row] = xv;
-    if (!POST) {
-      T u = P.sb[t] - P.sax[t];
-      r_out[row] = u - P.sd[t] * xv;
-    }
+  } else {
+    for (int t = threadIdx.x; t < m; t += blockDim.x) x_out[rs + t] = cur[t];
   }
 }
 
-
-// Register-resident variant for partitions of at most 1024 rows whose in-partition
-// rows have at most K entries: one thread per row keeps its entries (value, local
-// column) in registers across the sweeps, only x lives in shared memory.  Same
-// arithmetic and order as smooth_kernel.
+// Register-resident variant for groups of at most 512 rows whose in-partition rows
+// have at most K entries: one thread per row keeps its entries (value, 16-bit local
+// column) in registers across the sweeps; x is double-buffered in shared memory.
+// Same arithmetic and order as smooth_kernel with S = 1.
 template <class T, bool POST, int K>
 __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
-    const int32_t* __restrict__ part_idx, const int32_t* __restrict__ agg_idx, const int32_t* __restrict__ irp,
+    const int32_t* __restrict__ grows, const int32_t* __restrict__ irp,
     const int32_t* __restrict__ ici, const T* __restrict__ iv, const int32_t* __restrict__ orp,
     const int32_t* __restrict__ oci, const T* __restrict__ ov, const T* __restrict__ diag,
     const T* __restrict__ dinv, const T* __restrict__ b, T w, int inner, const T* __restrict__ x_in,
     T* __restrict__ x_out, T* __restrict__ r_out) {
   extern __shared__ __align__(16) unsigned char sm[];
-  T* sx = reinterpret_cast<T*>(sm);
-  const int rs = agg_idx[part_idx[blockIdx.x]], re = agg_idx[part_idx[blockIdx.x + 1]];
+  T* buf0 = reinterpret_cast<T*>(sm);
+  T* buf1 = buf0 + blockDim.x;
+  const int rs = grows[blockIdx.x], re = grows[blockIdx.x + 1];
   const int t = threadIdx.x;
   const bool live = t < re - rs;
   const int row = rs + t;
@@ -248,20 +254,24 @@ __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
       bb = b[row];
       x = (w * bb) * di;
     }
-    sx[t] = x;
+    buf0[t] = x;
   }
   __syncthreads();
+  T* src = buf0;
+  T* dst = buf1;
   for (int it = 0; it < inner; it++) {
-    T sax = 0;
-#pragma unroll
-    for (int k = 0; k < K; k++)
-      if (k < len) sax = sax + val[k] * sx[(colp[k >> 1] >> ((k & 1) * 16)) & 0xffffu];
-    __syncthreads();
     if (live) {
+      T sax = 0;
+#pragma unroll
+      for (int k = 0; k < K; k++)
+        if (k < len) sax = sax + val[k] * src[(colp[k >> 1] >> ((k & 1) * 16)) & 0xffffu];
       x = relax(x, bb, sax, d, di, w);
-      sx[t] = x;
+      dst[t] = x;
     }
     __syncthreads();
+    T* tmp = src;
+    src = dst;
+    dst = tmp;
   }
   if (live) {
     x_out[row] = x;
@@ -269,7 +279,7 @@ __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
       T sax = 0;
 #pragma unroll
       for (int k = 0; k < K; k++)
-        if (k < len) sax = sax + val[k] * sx[(colp[k >> 1] >> ((k & 1) * 16)) & 0xffffu];
+        if (k < len) sax = sax + val[k] * src[(colp[k >> 1] >> ((k & 1) * 16)) & 0xffffu];
       T u = bb - sax;
       r_out[row] = u - d * x;
     }
@@ -478,8 +488,6 @@ size_t smooth_smem(const Level<T>& L) {
 }
 
 
-constexpr int kRegRow = 16;
-
 // Lanes per row of the shared-memory smoother: 1024-thread CTAs, as many lanes per
 // row as the largest partition allows (the CPU oracle uses the same rule).
 inline int smem_lanes(int max_part_rows) {
@@ -514,10 +522,10 @@ void smooth(Ctx& c, Level<T>& L, bool post, const T* b, const T* xin, T* xout, T
   }
   const T w = (T)c.cfg.smootherWeight;
   const int inner = post ? c.cfg.postInnerIters : c.cfg.preInnerIters;
-  if (L.max_in_row <= kRegRow && L.max_part_rows <= 512) {
-    const int thr = ((L.max_part_rows + 31) / 32) * 32;
+  if (smoother_in_registers(L.max_in_row, L.max_part_rows)) {
+    const int thr = ((L.max_group_rows + 31) / 32) * 32;
     auto k = post ? smooth_reg_kernel<T, true, kRegRow> : smooth_reg_kernel<T, false, kRegRow>;
-    FG_LAUNCH(k, L.npart, thr < 32 ? 32 : thr, (size_t)thr * sizeof(T), s, L.part_idx.p, L.agg_idx.p, L.Ain.rp.p,
+    FG_LAUNCH(k, L.ngroups, thr < 32 ? 32 : thr, 2 * (size_t)thr * sizeof(T), s, L.grows.p, L.Ain.rp.p,
               L.Ain.ci.p, L.Ain.v.p, aorp, L.Aout.ci.p, L.Aout.v.p, L.diag.p, L.dinv.p, b, w, inner, xin, xout,
               rout);
     return;
@@ -525,8 +533,8 @@ void smooth(Ctx& c, Level<T>& L, bool post, const T* b, const T* xin, T* xout, T
   const size_t sm = smooth_smem(L);
   const bool st = staged(L);
   const int S = smem_lanes(L.max_part_rows);
-  using KFn = void (*)(const int32_t*, const int32_t*, const int32_t*, const int32_t*, const T*, const int32_t*,
-                       const int32_t*, const T*, const T*, const T*, const T*, T, int, const T*, T*, T*, int, int);
+  using KFn = void (*)(const int32_t*, const int32_t*, const int32_t*, const T*, const int32_t*, const int32_t*,
+                       const T*, const T*, const T*, const T*, T, int, const T*, T*, T*, int, int);
   KFn k;
 #define FG_SMOOTH_PICK(SS)                                                                  \
   k = post ? (st ? smooth_kernel<T, true, true, SS> : smooth_kernel<T, true, false, SS>)    \
@@ -542,7 +550,7 @@ void smooth(Ctx& c, Level<T>& L, bool post, const T* b, const T* xin, T* xout, T
 #undef FG_SMOOTH_PICK
   // the limit is a per-function attribute shared by every handle: set it per launch
   if (sm > 48 * 1024) FG_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  FG_LAUNCH(k, L.npart, 1024, sm, s, L.part_idx.p, L.agg_idx.p, L.Ain.rp.p, L.Ain.ci.p, L.Ain.v.p, aorp,
+  FG_LAUNCH(k, L.ngroups, 1024, sm, s, L.grows.p, L.Ain.rp.p, L.Ain.ci.p, L.Ain.v.p, aorp,
             L.Aout.ci.p, L.Aout.v.p, L.diag.p, L.dinv.p, b, w, inner, xin, xout, rout, L.max_part_rows,
             L.max_part_entries);
 }

@@ -53,11 +53,22 @@ struct Level {
   int max_part_rows = 0;
   int max_part_entries = 0;  // in-partition off-diagonal entries of the largest partition
   int max_in_row = 0;        // longest in-partition row
+  // smoother work groups: consecutive partitions packed per CTA (row offsets)
+  DBuf<int32_t> grows;
+  int ngroups = 0, max_group_rows = 0;
   // coarsest: explicit inverse, row-major n x n
   DBuf<double> Ainv;
   // work vectors (level numbering / permuted numbering)
   DBuf<T> b, x, r, xo, t, bp;  // bp: post-smoother right-hand side
 };
+
+// Level-0-style smoother in registers: rows of at most 16 in-partition entries and
+// partitions of at most 512 rows (one thread per row).
+constexpr int kRegRow = 16;
+constexpr int kRegGroupRows = 512;
+inline bool smoother_in_registers(int max_in_row, int max_part_rows) {
+  return max_in_row <= kRegRow && max_part_rows <= kRegGroupRows;
+}
 
 struct HierarchyBase {
   virtual ~HierarchyBase() {}
