@@ -147,6 +147,26 @@ femgpu_status femgpu_solve_device(femgpu_handle h, const double* d_b, double* d_
  * Replaces cusp::multiply(Ahyb_d_CG, ...) in cgcycle.cu:24,38. */
 femgpu_status femgpu_spmv_device(femgpu_handle h, const double* d_x, double* d_y);
 
+/* ---- allocation-free load vector ----------------------------------------------- */
+/* No reference counterpart.  Same result as femgpu_load_vector, but f and b are
+ * device arrays (nverts doubles, original numbering) and the call allocates no
+ * device memory.  It exists for callers that rebuild the right-hand side inside a
+ * time step and cannot allocate there: applications that hand almost all device
+ * memory to their own pool at start-up, or run under a fixed per-process memory
+ * cap, where a hidden allocation mid-step can fail.
+ * The two per-element scratch arrays live in a fixed region built into the
+ * library: 2 x FEMGPU_NOALLOC_MAX_ELEMENTS doubles (32 MiB) per device, reserved
+ * when this part of the library is first used.  Meshes with more elements are
+ * rejected with FEMGPU_ERR_LIMIT.  Nothing in the region has to start at zero:
+ * each call writes every slot it reads.
+ * The region is shared by every handle on a device, so calls that can overlap
+ * on one device (different streams or threads) race; calls on one stream are
+ * ordered.  The work is enqueued on the handle's stream and the call returns
+ * without waiting.  The first call on each device looks the region up (and may
+ * load this part of the library): make it before any stream capture begins. */
+#define FEMGPU_NOALLOC_MAX_ELEMENTS 2097152
+femgpu_status femgpu_load_vector_device_noalloc(femgpu_handle h, const double* d_f, double* d_b);
+
 /* ---- inspection (parity tests, statistics) --------------------------------- */
 /* Pattern/values of the assembled level-0 matrix (original numbering). Any
  * output pointer may be NULL; n and nnz are always written. */

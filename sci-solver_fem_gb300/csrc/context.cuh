@@ -120,6 +120,9 @@ struct Ctx {
 void build_mesh_pattern(Ctx& c);
 void assemble_operator(Ctx& c, const double* coef_host, double lambda);
 void load_vector(Ctx& c, const double* f_host, double* b_host);
+// The two load-vector passes on device f/b with caller-provided scratch (`scale`
+// and `fsum`, one double per element each); enqueued on c.stream, allocates nothing.
+void load_vector_enqueue(Ctx& c, const double* d_f, double* d_b, double* scale, double* fsum);
 void apply_dirichlet(Ctx& c, const uint8_t* mask_host);
 
 // amg_setup.cu

@@ -413,6 +413,14 @@ void load_vector(Ctx& c, const double* f_host, double* b_host) {
   FG_CUDA(cudaStreamSynchronize(s));
 }
 
+void load_vector_enqueue(Ctx& c, const double* d_f, double* d_b, double* scale, double* fsum) {
+  cudaStream_t s = c.stream;
+  Mesh& M = c.mesh;
+  FG_LAUNCH(element_load_kernel, grid_for(M.ne, 256), 256, 0, s, M.xyz.p, M.conn.p, d_f, M.ne, M.k, scale, fsum);
+  FG_LAUNCH(gather_load_kernel, grid_for(M.nv, 256), 256, 0, s, M.vstart.p, M.inc.p, scale, fsum, d_f, (int)M.nv,
+            M.k, d_b);
+}
+
 void apply_dirichlet(Ctx& c, const uint8_t* mask_host) {
   cudaStream_t s = c.stream;
   DBuf<uint8_t> mask(c.A.n, s);

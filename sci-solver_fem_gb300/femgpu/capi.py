@@ -25,7 +25,7 @@ EXPORTS = [
     "femgpu_set_mesh", "femgpu_assemble", "femgpu_load_vector", "femgpu_set_dirichlet", "femgpu_set_matrix_csr",
     "femgpu_setup", "femgpu_solve", "femgpu_solve_device", "femgpu_spmv_device", "femgpu_get_matrix",
     "femgpu_num_levels", "femgpu_get_level_info", "femgpu_level_get", "femgpu_vcycle", "femgpu_kernel_launches",
-    "femgpu_profile_kernel",
+    "femgpu_profile_kernel", "femgpu_load_vector_device_noalloc",
     "femgpu_read_tetgen", "femgpu_read_ply", "femgpu_read_mat_sparse", "femgpu_read_mat_array",
     "femgpu_write_mat_array", "femgpu_write_vtk",
 ]
@@ -95,6 +95,7 @@ def lib():
     L.femgpu_solve.argtypes = [_vp, _f64p, _f64p, C.POINTER(SolveStats)]
     L.femgpu_solve_device.argtypes = [_vp, _vp, _vp, C.POINTER(SolveStats)]
     L.femgpu_spmv_device.argtypes = [_vp, _vp, _vp]
+    L.femgpu_load_vector_device_noalloc.argtypes = [_vp, _vp, _vp]
     L.femgpu_get_matrix.argtypes = [_vp, _pi64, _pi64, _vp, _vp, _vp]
     L.femgpu_num_levels.argtypes = [_vp, C.POINTER(C.c_int)]
     L.femgpu_get_level_info.argtypes = [_vp, C.c_int, C.POINTER(LevelInfo)]
@@ -269,6 +270,13 @@ class Solver:
 
     def spmv_device(self, x_ptr: int, y_ptr: int):
         _check(lib().femgpu_spmv_device(self.h, _vp(x_ptr), _vp(y_ptr)), self.h)
+
+    def load_vector_device_noalloc(self, f_ptr: int, b_ptr: int, check=True):
+        """Device f -> device b on the handle's stream; allocates no device memory."""
+        status = lib().femgpu_load_vector_device_noalloc(self.h, _vp(f_ptr), _vp(b_ptr))
+        if check:
+            _check(status, self.h)
+        return status
 
 
 # ---- file IO -----------------------------------------------------------------------------
