@@ -66,6 +66,8 @@ typedef struct {
   int precision;            /* 0 = FP32 hierarchy in an FP64 outer PCG (reference), 1 = FP64 hierarchy */
   int flexibleCG;           /* 0 = Fletcher-Reeves beta (reference), 1 = Polak-Ribiere (flexible) */
   void* stream;             /* cudaStream_t to run on; NULL = library-owned stream */
+  void* mem_pool;           /* cudaMemPool_t for device buffers; NULL = a pool owned by the handle
+                               that keeps freed memory for reuse until femgpu_destroy */
 } femgpu_config;
 
 typedef struct {
@@ -88,7 +90,7 @@ void femgpu_config_default(femgpu_config* cfg);
  * (src/FEMSolver.cu:99-129), which the reference never calls. */
 femgpu_status femgpu_create(femgpu_handle* h, const femgpu_config* cfg);
 femgpu_status femgpu_destroy(femgpu_handle h);
-/* Replaces the options of an existing context (device and stream stay); the next
+/* Replaces the options of an existing context (device, stream and pool stay); the next
  * femgpu_setup uses them.  The reference reads its option members when solveFEM
  * constructs the AMG object (src/FEMSolver.cu:66-73). */
 femgpu_status femgpu_set_config(femgpu_handle h, const femgpu_config* cfg);

@@ -1138,8 +1138,12 @@ int setup_levels(orc_amg* h, std::vector<Level<T>>& L, const Csr<double>& A, con
       for (int i = 0; i < N; i++) max_row = std::max(max_row, lv.Ain.rp[i + 1] - lv.Ain.rp[i]);
       for (size_t q = 0; q + 1 < lv.partIdx.size(); q++)
         max_part = std::max(max_part, lv.aggIdx[lv.partIdx[q + 1]] - lv.aggIdx[lv.partIdx[q]]);
-      int sl = 1; /* 1024-thread CTAs: as many lanes per row as the largest partition allows */
-      while (sl < 32 && (int64_t)(sl * 2) * max_part <= 1024) sl <<= 1;
+      /* S lanes per row: doubled while every lane still adds >= 3 entries of an average
+       * row (ceil(in-partition nnz / N)) and N x lanes stays within 152 x 2048 */
+      const int64_t in_nnz = lv.Ain.rp[N];
+      const int64_t avg = N > 0 ? (in_nnz + N - 1) / N : 0;
+      int sl = 1;
+      while (sl < 32 && 3 * (2 * sl) <= avg && (int64_t)N * (2 * sl) <= 152LL * 2048) sl <<= 1;
       lv.smooth_lanes = (max_row <= 16 && max_part <= 512) ? 1 : sl;
     }
     lv.P = build_prolongator(lv.Ap, lv.diag, lv.aggOf, nagg, c.pro_omega);
@@ -1174,14 +1178,14 @@ inline T relax_update(T x, T b, T sAx, T d, T dinv, T w) {
 }
 
 /* Row sum of in-partition entries in the device's lane order: S lanes, lane j takes
- * entries j, j+S, ... (products rounded, then added), then an xor butterfly. */
+ * entries j, j+S, ... with fused multiply-adds, then an xor butterfly. */
 template <class T>
 inline T part_row_sum(const Csr<T>& M, int i, const T* x, int xoff, int S) {
   T p[32], q[32];
   for (int j = 0; j < S; j++) p[j] = 0;
   for (int e = M.rp[i]; e < M.rp[i + 1]; e++) {
     int j = (e - M.rp[i]) % S;
-    p[j] = p[j] + M.v[e] * x[M.ci[e] - xoff];
+    p[j] = std::fma(M.v[e], x[M.ci[e] - xoff], p[j]);
   }
   for (int off = S >> 1; off > 0; off >>= 1) {
     for (int j = 0; j < S; j++) q[j] = p[j] + p[j ^ off];

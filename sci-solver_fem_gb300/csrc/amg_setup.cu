@@ -351,6 +351,7 @@ void aggregate(Ctx& c, int n, const int32_t* xadj, const int32_t* adj, int depth
     int32_t h[2];
     counters.download(h, 2);
     FG_CUDA(cudaStreamSynchronize(s));
+    g_host_syncs.fetch_add(1, std::memory_order_relaxed);
     if (h[0] == 0) {
       if (!weighted) {
         if (remove_small_parts(c, n, part, nullptr, 0, min_size, full_size, aggregated) == 0) return;
@@ -455,19 +456,26 @@ struct PhaseTimer {
   cudaStream_t s;
   int level;
   std::chrono::steady_clock::time_point t0;
+  int64_t syncs0 = 0, launches0 = 0;
   PhaseTimer(cudaStream_t st, int lvl) : on(getenv("FEMGPU_PROFILE") != nullptr), s(st), level(lvl) {
     if (on) {
       cudaStreamSynchronize(s);
       t0 = std::chrono::steady_clock::now();
+      syncs0 = g_host_syncs.load();
+      launches0 = g_kernel_launches.load();
     }
   }
   void mark(const char* what) {
     if (!on) return;
     cudaStreamSynchronize(s);
     auto t = std::chrono::steady_clock::now();
-    fprintf(stderr, "[femgpu setup] level %d %-10s %8.3f ms\n", level, what,
-            std::chrono::duration<double, std::milli>(t - t0).count());
+    const int64_t sy = g_host_syncs.load(), la = g_kernel_launches.load();
+    fprintf(stderr, "[femgpu setup] level %d %-10s %8.3f ms  %5lld launches %4lld host reads\n", level, what,
+            std::chrono::duration<double, std::milli>(t - t0).count(), (long long)(la - launches0),
+            (long long)(sy - syncs0));
     t0 = t;
+    syncs0 = sy;
+    launches0 = la;
   }
 };
 
@@ -1571,6 +1579,13 @@ __global__ void partition_starts_kernel(int npart, const int32_t* part_idx, cons
   }
 }
 
+// In-partition columns relative to the first row of their group (one CTA per group).
+__global__ void group_local_cols_kernel(const int32_t* grows, const int32_t* irp, const int32_t* ici,
+                                        uint16_t* c16) {
+  const int rs = grows[blockIdx.x], re = grows[blockIdx.x + 1];
+  for (int q = irp[rs] + threadIdx.x; q < irp[re]; q += blockDim.x) c16[q] = (uint16_t)(ici[q] - rs);
+}
+
 // Smoother work groups: consecutive partitions packed greedily into one CTA while
 // the group stays within `max_rows` rows and `max_ents` in-partition entries.
 template <class T>
@@ -1581,17 +1596,19 @@ void build_smoother_groups(Ctx& c, Level<T>& L, int max_rows, int max_ents) {
             L.Ain.rp.p, row0.p, ent0.p);
   std::vector<int32_t> hr = row0.to_host(), he = ent0.to_host();
   std::vector<int32_t> g{hr[0]};
-  int gp = 0, mx = 0;
+  int gp = 0, mx = 0, mxe = 0;
   for (int p = 1; p <= L.npart; p++) {
     const bool last = p == L.npart;
     if (last || hr[p + 1] - hr[gp] > max_rows || he[p + 1] - he[gp] > max_ents) {
       g.push_back(hr[p]);
       mx = std::max(mx, hr[p] - hr[gp]);
+      mxe = std::max(mxe, he[p] - he[gp]);
       gp = p;
     }
   }
   L.ngroups = (int)g.size() - 1;
   L.max_group_rows = mx;
+  L.max_group_ents = mxe;
   L.grows.alloc(g.size(), s);
   L.grows.upload(g.data(), g.size());
 }
@@ -1677,7 +1694,8 @@ void build_levels(Ctx& c, Hierarchy<T>& H) {
       L.Ain.nnz = exclusive_scan(cin.p, L.Ain.rp.p, N, s);
       L.Aout.nnz = exclusive_scan(cout.p, L.Aout.rp.p, N, s);
       L.Ain.ci.alloc(L.Ain.nnz > 0 ? L.Ain.nnz : 1, s);
-      L.Ain.v.alloc(L.Ain.nnz > 0 ? L.Ain.nnz : 1, s);
+      L.Ain.v.alloc(L.Ain.nnz + 16, s);  // slack for 16-byte rounded bulk copies
+      L.Ain.v.zero();
       L.Aout.ci.alloc(L.Aout.nnz > 0 ? L.Aout.nnz : 1, s);
       L.Aout.v.alloc(L.Aout.nnz > 0 ? L.Aout.nnz : 1, s);
       FG_LAUNCH(split_fill_kernel<T>, grid_for(N, 256), 256, 0, s, N, L.Ap.rp.p, L.Ap.ci.p, L.Ap.v.p,
@@ -1693,10 +1711,22 @@ void build_levels(Ctx& c, Hierarchy<T>& H) {
       DBuf<int32_t> rlen(N + 1, s);
       FG_LAUNCH(row_lengths_kernel, grid_for(N, 256), 256, 0, s, N, L.Ain.rp.p, rlen.p);
       L.max_in_row = reduce_max(rlen.p, N, s);
-      if (smoother_in_registers(L.max_in_row, L.max_part_rows))
+      if (smoother_in_registers(L.max_in_row, L.max_part_rows)) {
         build_smoother_groups(c, L, kRegGroupRows, std::numeric_limits<int>::max());
-      else
+        L.ci16.alloc(L.Ain.nnz + 16, s);
+        L.ci16.zero();
+        if (L.ngroups > 0)
+          FG_LAUNCH(group_local_cols_kernel, L.ngroups, 256, 0, s, L.grows.p, L.Ain.rp.p, L.Ain.ci.p, L.ci16.p);
+      } else
         build_smoother_groups(c, L, L.max_part_rows, L.max_part_entries);
+      plan_smoother(c, L);
+      if (pt.on)
+        fprintf(stderr,
+                "[femgpu setup] level %d smoother: %s, groups %d (max %d rows), lanes %d, cluster %d, "
+                "slice %d rows / %d entries, %d threads, %zu B shared%s\n",
+                num_levels - 1, smoother_in_registers(L.max_in_row, L.max_part_rows) ? "registers" : "cluster",
+                L.ngroups, L.max_group_rows, L.smooth_lanes, L.cluster, L.slice_rows, L.slice_ents,
+                L.smooth_threads, L.smooth_smem, L.smooth_staged ? ", staged" : "");
     }
     pt.mark("split");
     // prolongator and restrictor
@@ -1781,6 +1811,8 @@ __global__ void identity_kernel(int n, int32_t* p) {
 }  // namespace
 
 std::atomic<int64_t> g_kernel_launches{0};
+std::atomic<int64_t> g_host_syncs{0};
+thread_local cudaMemPool_t g_alloc_pool = nullptr;
 
 void amg_setup(Ctx& c) {
   cudaStream_t s = c.stream;

@@ -4,15 +4,20 @@
 // One CTA per partition keeps the partition's x in shared memory and runs the
 // inner weighted-Jacobi sweeps over in-partition couplings; cross-partition
 // couplings enter once per relax (pre: preRRSym_kernel + preAout_kernel,
-// gauss_seidel.cu:1278-2015; post: postRelaxSym_kernel, :3626-3736).  Row sums
-// run in ascending column order with separately rounded products (the reference
+// gauss_seidel.cu:1278-2015; post: postRelaxSym_kernel, :3626-3736).  In-partition
+// row sums run in a fixed lane order with fused multiply-adds (the reference
 // accumulates in shared-memory atomics in arbitrary order).
 //
 // PCG (CG_Flex_Cycle, cgcycle.cu:6-69) runs in FP64 on the level-0 permuted
 // numbering: b is permuted on entry and x back on exit, so the solved system is
 // A x = b (the reference applies the permuted operator to unpermuted vectors).
 // Reductions are two-stage with a fixed grid, so results are bitwise reproducible.
+#include <algorithm>
 #include <cmath>
+
+#include <cooperative_groups.h>
+
+namespace cg = cooperative_groups;
 
 #include "context.cuh"
 
@@ -25,7 +30,7 @@ constexpr int kRedThreads = 256;
 
 // device scalar slots in Ctx::red (after the partials)
 enum Slot {
-  S_BN = 0, S_NR, S_YP, S_ALPHA, S_RZ, S_RZNEW, S_ZROLD, S_BETA, S_FLAG, S_FIRST, S_COUNT
+  S_BN = 0, S_NR, S_YP, S_ALPHA, S_RZ, S_RZNEW, S_ZROLD, S_BETA, S_FLAG, S_FIRST, S_KERR, S_COUNT
 };
 
 __device__ __forceinline__ double block_sum(double v, double* sh) {
@@ -81,48 +86,50 @@ __device__ __forceinline__ T relax(T x, T b, T sax, T d, T dinv, T w) {
   return x + (w * t) * dinv;
 }
 
-// Shared-memory layout of one partition in the smoother: x, the in-partition sums,
-// the right-hand side, the diagonal, local row offsets and (when it fits) the
-// partition's block of in-partition entries with 16-bit local column indices.
+// Shared-memory layout of one CTA of the cluster smoother: the whole group's x
+// (double-buffered), then for the CTA's own row slice the right-hand side, the
+// diagonal and its reciprocal, local row offsets and (when they fit) the slice's
+// in-partition entries with 16-bit column indices local to the group.
 template <class T>
-struct PartSmem {
-  T *sx, *sax, *sb, *sd, *sdi, *sval;
+struct SliceSmem {
+  T *xa, *xb, *sb, *sd, *sdi, *sval;
   int32_t* srp;
   uint16_t* scol;
 };
 
 template <class T>
-__device__ __forceinline__ PartSmem<T> carve(unsigned char* sm, int mcap, int ecap) {
-  PartSmem<T> L;
-  L.sx = reinterpret_cast<T*>(sm);
-  L.sax = L.sx + mcap;
-  L.sb = L.sax + mcap;
-  L.sd = L.sb + mcap;
-  L.sdi = L.sd + mcap;
-  L.sval = L.sdi + mcap;
+__device__ __forceinline__ SliceSmem<T> carve(unsigned char* sm, int mcap, int scap, int ecap) {
+  SliceSmem<T> L;
+  L.xa = reinterpret_cast<T*>(sm);
+  L.xb = L.xa + mcap;
+  L.sb = L.xb + mcap;
+  L.sd = L.sb + scap;
+  L.sdi = L.sd + scap;
+  L.sval = L.sdi + scap;
   L.srp = reinterpret_cast<int32_t*>(L.sval + ecap);
-  L.scol = reinterpret_cast<uint16_t*>(L.srp + mcap + 1);
+  L.scol = reinterpret_cast<uint16_t*>(L.srp + scap + 1);
   return L;
 }
 
 template <class T>
-size_t part_smem_bytes(int mcap, int ecap) {
-  return (size_t)mcap * 5 * sizeof(T) + (size_t)ecap * sizeof(T) + (size_t)(mcap + 1) * 4 + (size_t)ecap * 2 + 16;
+size_t slice_smem_bytes(int mcap, int scap, int ecap) {
+  return (size_t)mcap * 2 * sizeof(T) + (size_t)scap * 3 * sizeof(T) + (size_t)ecap * sizeof(T) +
+         (size_t)(scap + 1) * 4 + (size_t)ecap * 2 + 16;
 }
 
-// Sum over row t's in-partition entries with S lanes per row: lane j adds entries
-// j, j+S, ... in order (products rounded separately; the reference adds them with
-// shared-memory atomics in any order), then an xor butterfly combines the lanes.
-// Every lane of the warp must call it (the butterfly shuffles the whole warp).
+// Sum over slice row t's in-partition entries with S lanes per row: lane j adds
+// entries j, j+S, ... in order with fused multiply-adds (the reference adds them with
+// shared-memory atomics in any order), then an xor butterfly combines the lanes.  Every lane of the warp must call it (the butterfly shuffles the warp).
 template <class T, bool STAGED, int S>
-__device__ __forceinline__ T part_row_sum(const PartSmem<T>& P, int t, bool live, int j,
-                                          const int32_t* __restrict__ ici, const T* __restrict__ iv, int es, int rs) {
+__device__ __forceinline__ T slice_row_sum(const SliceSmem<T>& P, const T* x, int t, bool live, int j,
+                                           const int32_t* __restrict__ ici, const T* __restrict__ iv, int es,
+                                           int rs) {
   T s = 0;
   if (live) {
     const int q0 = P.srp[t], q1 = P.srp[t + 1];
     for (int q = q0 + j; q < q1; q += S) {
-      if (STAGED) s = s + P.sval[q] * P.sx[P.scol[q]];
-      else s = s + iv[es + q] * P.sx[ici[es + q] - rs];
+      if (STAGED) s = fma(P.sval[q], x[P.scol[q]], s);
+      else s = fma(iv[es + q], x[ici[es + q] - rs], s);
     }
   }
 #pragma unroll
@@ -130,10 +137,13 @@ __device__ __forceinline__ T part_row_sum(const PartSmem<T>& P, int t, bool live
   return s;
 }
 
-// Partition-block Jacobi smoother.  One CTA runs a group of consecutive partitions
-// (rows [grows[g], grows[g+1])): in-partition entries never leave their partition,
-// so a group of partitions is smoothed exactly like each partition on its own.
-// x is double-buffered in shared memory (one barrier per sweep).
+// Partition-block Jacobi smoother on thread-block clusters.  A cluster of C CTAs
+// runs one group of consecutive partitions (rows [grows[g], grows[g+1])): in-partition
+// entries never leave their partition, so a group is smoothed exactly like each of
+// its partitions alone.  CTA c of the cluster owns a slice of ceil(m / C) rows; every
+// CTA keeps the whole group's x, and after each sweep a row's new value is stored
+// into all C copies through distributed shared memory, then one cluster barrier
+// ends the sweep (x is double-buffered).
 // POST == false (preRRSym_kernel + the in-partition part of the residual,
 //   gauss_seidel.cu:1278-1376): x0 = w b / d, `inner` sweeps, then x and
 //   r = b - A_in x - d x are written;
@@ -141,148 +151,227 @@ __device__ __forceinline__ T part_row_sum(const PartSmem<T>& P, int t, bool live
 //   (precomputed by aout_rhs_kernel when orp == nullptr), `inner` sweeps from x_in,
 //   result written to x_out.
 template <class T, bool POST, bool STAGED, int S>
-__global__ void __launch_bounds__(1024) smooth_kernel(
+__global__ void __launch_bounds__(1024) smooth_cluster_kernel(
     const int32_t* __restrict__ grows, const int32_t* __restrict__ irp,
     const int32_t* __restrict__ ici, const T* __restrict__ iv, const int32_t* __restrict__ orp,
     const int32_t* __restrict__ oci, const T* __restrict__ ov, const T* __restrict__ diag,
     const T* __restrict__ dinv, const T* __restrict__ b, T w, int inner, const T* __restrict__ x_in,
-    T* __restrict__ x_out, T* __restrict__ r_out, int mcap, int ecap) {
+    T* __restrict__ x_out, T* __restrict__ r_out, int mcap, int scap, int ecap) {
   extern __shared__ __align__(16) unsigned char sm[];
-  const int rs = grows[blockIdx.x], re = grows[blockIdx.x + 1];
-  const int m = re - rs;
-  const int es = irp[rs], ne = irp[re] - es;
-  PartSmem<T> P = carve<T>(sm, mcap, STAGED ? ecap : 0);
+  cg::cluster_group cl = cg::this_cluster();
+  const int C = (int)cl.num_blocks();
+  const int c = (int)cl.block_rank();
+  const int g = blockIdx.x / C;
+  const int rs = grows[g], m = grows[g + 1] - rs;
+  const int qs = (m + C - 1) / C;
+  const int ss = min(m, c * qs), ns = min(m, ss + qs) - ss;  // own slice: group rows [ss, ss + ns)
+  const int es = irp[rs + ss], ne = irp[rs + ss + ns] - es;
+  SliceSmem<T> P = carve<T>(sm, mcap, scap, STAGED ? ecap : 0);
   for (int t = threadIdx.x; t < m; t += blockDim.x) {
     const int row = rs + t;
-    const T d = diag[row], di = dinv[row];
-    P.sd[t] = d;
-    P.sdi[t] = di;
-    P.srp[t] = irp[row] - es;
-    if (POST) {
-      T acc = b[row];
-      if (orp)
-        for (int e = orp[row]; e < orp[row + 1]; e++) acc = acc + (-ov[e]) * x_in[oci[e]];
-      P.sb[t] = acc;
-      P.sx[t] = x_in[row];
-    } else {
-      const T bv = b[row];
-      P.sb[t] = bv;
-      P.sx[t] = (w * bv) * di;
-    }
+    P.xa[t] = POST ? x_in[row] : (w * b[row]) * dinv[row];
   }
-  if (threadIdx.x == 0) P.srp[m] = ne;
+  for (int t = threadIdx.x; t < ns; t += blockDim.x) {
+    const int row = rs + ss + t;
+    P.sd[t] = diag[row];
+    P.sdi[t] = dinv[row];
+    P.srp[t] = irp[row] - es;
+    T acc = b[row];
+    if (POST && orp)
+      for (int e = orp[row]; e < orp[row + 1]; e++) acc = acc + (-ov[e]) * x_in[oci[e]];
+    P.sb[t] = acc;
+  }
+  if (threadIdx.x == 0) P.srp[ns] = ne;
   if (STAGED)
     for (int q = threadIdx.x; q < ne; q += blockDim.x) {
       P.sval[q] = iv[es + q];
       P.scol[q] = (uint16_t)(ici[es + q] - rs);
     }
-  __syncthreads();
+  cl.sync();  // every CTA of the cluster is running and holds x0
   const int j = threadIdx.x & (S - 1), per = blockDim.x / S;
-  T* cur = P.sx;
-  T* nxt = P.sax;
+  T* cur = P.xa;
+  T* nxt = P.xb;
   for (int it = 0; it < inner; it++) {
-    P.sx = cur;
-    for (int base = 0; base < m; base += per) {
+    for (int base = 0; base < ns; base += per) {
       const int t = base + threadIdx.x / S;
-      const T v = part_row_sum<T, STAGED, S>(P, t, t < m, j, ici, iv, es, rs);
-      if (j == 0 && t < m) nxt[t] = relax(cur[t], P.sb[t], v, P.sd[t], P.sdi[t], w);
+      const bool live = t < ns;
+      const T v = slice_row_sum<T, STAGED, S>(P, cur, t, live, j, ici, iv, es, rs);
+      if (j == 0 && live) {
+        const T xn = relax(cur[ss + t], P.sb[t], v, P.sd[t], P.sdi[t], w);
+        for (int r = 0; r < C; r++) *cl.map_shared_rank(nxt + ss + t, r) = xn;
+      }
     }
-    __syncthreads();
+    cl.sync();  // all copies of the new x written; the old buffer is no longer read
     T* tmp = cur;
     cur = nxt;
     nxt = tmp;
   }
-  P.sx = cur;
   if (!POST) {
-    for (int base = 0; base < m; base += per) {
+    for (int base = 0; base < ns; base += per) {
       const int t = base + threadIdx.x / S;
-      const T v = part_row_sum<T, STAGED, S>(P, t, t < m, j, ici, iv, es, rs);
-      if (j == 0 && t < m) {
-        const T xv = cur[t];
-        x_out[rs + t] = xv;
+      const bool live = t < ns;
+      const T v = slice_row_sum<T, STAGED, S>(P, cur, t, live, j, ici, iv, es, rs);
+      if (j == 0 && live) {
+        const T xv = cur[ss + t];
+        x_out[rs + ss + t] = xv;
         T u = P.sb[t] - v;
-        r_out[rs + t] = u - P.sd[t] * xv;
+        r_out[rs + ss + t] = u - P.sd[t] * xv;
       }
     }
   } else {
-    for (int t = threadIdx.x; t < m; t += blockDim.x) x_out[rs + t] = cur[t];
+    for (int t = threadIdx.x; t < ns; t += blockDim.x) x_out[rs + ss + t] = cur[ss + t];
   }
 }
 
-// Register-resident variant for groups of at most 512 rows whose in-partition rows
-// have at most K entries: one thread per row keeps its entries (value, 16-bit local
-// column) in registers across the sweeps; x is double-buffered in shared memory.
-// Same arithmetic and order as smooth_kernel with S = 1.
+// Shared memory of the register smoother: two mbarriers, x twice (kRegGroupRows + 1
+// slots each; the last slot stays 0 for padded entries), then two staging buffers for
+// a group's in-partition values and 16-bit local columns (ecap entries each, filled
+// as 16-byte rounded ranges).
+struct RegSmemLayout {
+  size_t x0, x1, val0, col0, val1, col1, total;
+};
+
+template <class T>
+__host__ __device__ constexpr size_t round16(size_t v) {
+  return (v + 15) / 16 * 16;
+}
+
+template <class T>
+__host__ __device__ inline RegSmemLayout reg_smem_layout(int ecap) {
+  RegSmemLayout L{};
+  L.x0 = 16;
+  L.x1 = L.x0 + (size_t)(kRegGroupRows + 1) * sizeof(T);
+  L.val0 = round16<T>(L.x1 + (size_t)(kRegGroupRows + 1) * sizeof(T));
+  L.col0 = round16<T>(L.val0 + (size_t)ecap * sizeof(T));
+  L.val1 = round16<T>(L.col0 + (size_t)ecap * 2);
+  L.col1 = round16<T>(L.val1 + (size_t)ecap * sizeof(T));
+  L.total = round16<T>(L.col1 + (size_t)ecap * 2);
+  return L;
+}
+
+// One thread (thread 0) starts the bulk copies of group g's values and columns into
+// staging buffer `buf`; completion is counted on bar[buf].
+template <class T>
+__device__ __forceinline__ void stage_group(unsigned char* sm, const RegSmemLayout& Ls, uint64_t* bar, int buf,
+                                            int g, const int32_t* __restrict__ grows,
+                                            const int32_t* __restrict__ irp, const uint16_t* __restrict__ c16,
+                                            const T* __restrict__ iv) {
+  constexpr int VA = 16 / (int)sizeof(T);
+  const int es = irp[grows[g]], ee = irp[grows[g + 1]];
+  const int v0 = es & ~(VA - 1), c0 = es & ~7;
+  const uint32_t vbytes = (uint32_t)((((ee + VA - 1) & ~(VA - 1)) - v0) * (int)sizeof(T));
+  const uint32_t cbytes = (uint32_t)((((ee + 7) & ~7) - c0) * 2);
+  mbar_arrive_expect_tx(bar + buf, vbytes + cbytes);
+  if (vbytes) bulk_copy_g2s(sm + (buf ? Ls.val1 : Ls.val0), iv + v0, vbytes, bar + buf);
+  if (cbytes) bulk_copy_g2s(sm + (buf ? Ls.col1 : Ls.col0), c16 + c0, cbytes, bar + buf);
+}
+
+// Register-resident smoother for groups of at most 512 rows whose in-partition rows
+// have at most K entries: one thread per row, persistent CTAs walking the groups.
+// A group's values and 16-bit local columns are contiguous in HBM; thread 0 moves the
+// NEXT group's ranges into the other staging buffer with bulk asynchronous copies
+// (TMA) while the CTA smooths the current one.  Each thread keeps its row's entries
+// (padded to K with zero values pointing at a zero slot of x) in registers across the
+// sweeps; x is double-buffered in shared memory (one barrier per sweep).  Row sums
+// are the one-lane case of the shared-memory smoother: fused multiply-adds in entry
+// order.  A copy that does not land within the wait limit sets *kerr and ends the CTA.
 template <class T, bool POST, int K>
 __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
-    const int32_t* __restrict__ grows, const int32_t* __restrict__ irp,
-    const int32_t* __restrict__ ici, const T* __restrict__ iv, const int32_t* __restrict__ orp,
-    const int32_t* __restrict__ oci, const T* __restrict__ ov, const T* __restrict__ diag,
+    int ngroups, const int32_t* __restrict__ grows, const int32_t* __restrict__ irp,
+    const uint16_t* __restrict__ c16, const T* __restrict__ iv, const T* __restrict__ diag,
     const T* __restrict__ dinv, const T* __restrict__ b, T w, int inner, const T* __restrict__ x_in,
-    T* __restrict__ x_out, T* __restrict__ r_out) {
-  extern __shared__ __align__(16) unsigned char sm[];
-  T* buf0 = reinterpret_cast<T*>(sm);
-  T* buf1 = buf0 + blockDim.x;
-  const int rs = grows[blockIdx.x], re = grows[blockIdx.x + 1];
+    T* __restrict__ x_out, T* __restrict__ r_out, int ecap, double* __restrict__ kerr) {
+  extern __shared__ __align__(128) unsigned char sm[];
+  const RegSmemLayout Ls = reg_smem_layout<T>(ecap);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm);
+  T* const xa = reinterpret_cast<T*>(sm + Ls.x0);
+  T* const xb = reinterpret_cast<T*>(sm + Ls.x1);
+  constexpr int kZero = kRegGroupRows;  // x slot that stays 0
+  constexpr int VA = 16 / (int)sizeof(T);
   const int t = threadIdx.x;
-  const bool live = t < re - rs;
-  const int row = rs + t;
-  T val[K];
-  uint32_t colp[K / 2];  // two 16-bit local columns per register
-  int len = 0;
-  T d = (T)1, di = (T)1, bb = (T)0, x = (T)0;
-  if (live) {
-    const int e0 = irp[row];
-    len = irp[row + 1] - e0;
-#pragma unroll
-    for (int k = 0; k < K; k += 2) {
-      val[k] = k < len ? iv[e0 + k] : (T)0;
-      val[k + 1] = k + 1 < len ? iv[e0 + k + 1] : (T)0;
-      const uint32_t c0 = k < len ? (uint32_t)(ici[e0 + k] - rs) : 0u;
-      const uint32_t c1 = k + 1 < len ? (uint32_t)(ici[e0 + k + 1] - rs) : 0u;
-      colp[k >> 1] = c0 | (c1 << 16);
-    }
-    d = diag[row];
-    di = dinv[row];
-    if (POST) {
-      T acc = b[row];
-      if (orp)
-        for (int e = orp[row]; e < orp[row + 1]; e++) acc = acc + (-ov[e]) * x_in[oci[e]];
-      bb = acc;
-      x = x_in[row];
-    } else {
-      bb = b[row];
-      x = (w * bb) * di;
-    }
-    buf0[t] = x;
+  if (t == 0) {
+    mbar_init(bar, 1);
+    mbar_init(bar + 1, 1);
+    xa[kZero] = (T)0;
+    xb[kZero] = (T)0;
   }
   __syncthreads();
-  T* src = buf0;
-  T* dst = buf1;
-  for (int it = 0; it < inner; it++) {
+  if (t == 0 && (int)blockIdx.x < ngroups) stage_group<T>(sm, Ls, bar, 0, blockIdx.x, grows, irp, c16, iv);
+  int i = 0;
+  for (int g = blockIdx.x; g < ngroups; g += gridDim.x, i++) {
+    const int buf = i & 1;
+    const uint32_t parity = (uint32_t)(i >> 1) & 1u;
+    const int gn = g + gridDim.x;
+    // buffer buf ^ 1 was last read before the barrier that ended the previous group
+    if (t == 0 && gn < ngroups) stage_group<T>(sm, Ls, bar, buf ^ 1, gn, grows, irp, c16, iv);
+    const int rs = grows[g], re = grows[g + 1];
+    const bool live = t < re - rs;
+    const int row = rs + t;
+    int e0 = 0, len = 0;
+    T d = (T)1, di = (T)1, bb = (T)0, x = (T)0;
     if (live) {
-      T sax = 0;
-#pragma unroll
-      for (int k = 0; k < K; k++)
-        if (k < len) sax = sax + val[k] * src[(colp[k >> 1] >> ((k & 1) * 16)) & 0xffffu];
-      x = relax(x, bb, sax, d, di, w);
-      dst[t] = x;
+      e0 = irp[row];
+      len = irp[row + 1] - e0;
+      d = diag[row];
+      di = dinv[row];
+      bb = b[row];
+      x = POST ? x_in[row] : (w * bb) * di;
+      xa[t] = x;
     }
-    __syncthreads();
-    T* tmp = src;
-    src = dst;
-    dst = tmp;
-  }
-  if (live) {
-    x_out[row] = x;
-    if (!POST) {
-      T sax = 0;
+    const bool ok = mbar_wait_bounded(bar + buf, parity);
+    T val[K];
+    uint32_t off[K];
+    {
+      const int es = irp[rs];
+      const T* sval = reinterpret_cast<const T*>(sm + (buf ? Ls.val1 : Ls.val0)) + (e0 - (es & ~(VA - 1)));
+      const uint16_t* scol = reinterpret_cast<const uint16_t*>(sm + (buf ? Ls.col1 : Ls.col0)) + (e0 - (es & ~7));
 #pragma unroll
-      for (int k = 0; k < K; k++)
-        if (k < len) sax = sax + val[k] * src[(colp[k >> 1] >> ((k & 1) * 16)) & 0xffffu];
-      T u = bb - sax;
-      r_out[row] = u - d * x;
+      for (int k = 0; k < K; k++) {
+        const bool a = ok && k < len;
+        val[k] = a ? sval[k] : (T)0;
+        off[k] = a ? (uint32_t)scol[k] : (uint32_t)kZero;
+      }
     }
+    if (__syncthreads_or(!ok)) {
+      if (t == 0) {
+        *kerr = 1.0;
+        // let the copies in flight land before the CTA exits
+        (void)mbar_wait_bounded(bar + buf, parity);
+        if (gn < ngroups) (void)mbar_wait_bounded(bar + (buf ^ 1), (uint32_t)((i + 1) >> 1) & 1u);
+      }
+      return;
+    }
+    auto sweep = [&](const T* src, T* dst) {
+      if (live) {
+        T sax = 0;
+#pragma unroll
+        for (int k = 0; k < K; k++) sax = fma(val[k], src[off[k]], sax);
+        x = relax(x, bb, sax, d, di, w);
+        dst[t] = x;
+      }
+      __syncthreads();
+    };
+    int it = 0;
+    for (; it + 1 < inner; it += 2) {
+      sweep(xa, xb);
+      sweep(xb, xa);
+    }
+    const T* last = xa;
+    if (it < inner) {
+      sweep(xa, xb);
+      last = xb;
+    }
+    if (live) {
+      x_out[row] = x;
+      if (!POST) {
+        T sax = 0;
+#pragma unroll
+        for (int k = 0; k < K; k++) sax = fma(val[k], last[off[k]], sax);
+        T u = bb - sax;
+        r_out[row] = u - d * x;
+      }
+    }
+    __syncthreads();  // x buffers and this staging buffer are free for the next group
   }
 }
 
@@ -453,6 +542,8 @@ __global__ void perm_vec_out_kernel(int n, const int32_t* perm, const double* in
 
 // ---- V-cycle driver ------------------------------------------------------------------
 constexpr size_t kStageLimit = 200 * 1024;  // staged smoother: one 1024-thread CTA per SM
+constexpr size_t kSmemOptIn = 227 * 1024;   // largest dynamic shared memory of one CTA
+constexpr int kMaxCluster = 8;              // portable thread-block cluster size
 
 // Lanes per row for the R/P products: the same rule in the CPU oracle.
 inline int lanes_for_rows(int64_t nnz, int n) {
@@ -478,22 +569,55 @@ void spmv_lanes(const DCsr<T>& M, const T* x, T* y, int accumulate, cudaStream_t
 }
 
 template <class T>
-bool staged(const Level<T>& L) {
-  return L.max_part_rows < 65536 && part_smem_bytes<T>(L.max_part_rows, L.max_part_entries) <= kStageLimit;
-}
+using ClusterSmoothFn = void (*)(const int32_t*, const int32_t*, const int32_t*, const T*, const int32_t*,
+                                 const int32_t*, const T*, const T*, const T*, const T*, T, int, const T*, T*, T*, int,
+                                 int, int);
 
 template <class T>
-size_t smooth_smem(const Level<T>& L) {
-  return part_smem_bytes<T>(L.max_part_rows, staged(L) ? L.max_part_entries : 0);
+ClusterSmoothFn<T> pick_cluster_kernel(bool post, bool staged, int S) {
+#define FG_SMOOTH_PICK(SS)                                                                              \
+  return post ? (staged ? smooth_cluster_kernel<T, true, true, SS> : smooth_cluster_kernel<T, true, false, SS>) \
+              : (staged ? smooth_cluster_kernel<T, false, true, SS> : smooth_cluster_kernel<T, false, false, SS>)
+  switch (S) {
+    case 1: FG_SMOOTH_PICK(1);
+    case 2: FG_SMOOTH_PICK(2);
+    case 4: FG_SMOOTH_PICK(4);
+    case 8: FG_SMOOTH_PICK(8);
+    case 16: FG_SMOOTH_PICK(16);
+    default: FG_SMOOTH_PICK(32);
+  }
+#undef FG_SMOOTH_PICK
 }
 
+// Launch with a 1-D thread-block cluster of `cluster` CTAs (counted like FG_LAUNCH).
+template <class... KArgs, class... Args>
+void launch_clustered(void (*k)(KArgs...), int grid, int block, size_t smem, int cluster, cudaStream_t s,
+                      Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = (unsigned)cluster;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
+  FG_CUDA(cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...));
+}
 
-// Lanes per row of the shared-memory smoother: 1024-thread CTAs, as many lanes per
-// row as the largest partition allows (the CPU oracle uses the same rule).
-inline int smem_lanes(int max_part_rows) {
-  int s = 1;
-  while (s < 32 && (int64_t)(s * 2) * max_part_rows <= 1024) s <<= 1;
-  return s;
+// Entries of each CTA's row slice when groups are split over `C` CTAs.
+__global__ void slice_entries_kernel(int ngroups, int C, const int32_t* grows, const int32_t* irp, int32_t* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ngroups * C) return;
+  const int g = i / C, c = i % C;
+  const int rs = grows[g], m = grows[g + 1] - rs;
+  const int qs = (m + C - 1) / C;
+  const int ss = min(m, c * qs), se = min(m, ss + qs);
+  out[i] = irp[rs + se] - irp[rs + ss];
 }
 
 // Post-smoother right-hand side b' = b - A_out x (the first loop of
@@ -523,36 +647,32 @@ void smooth(Ctx& c, Level<T>& L, bool post, const T* b, const T* xin, T* xout, T
   const T w = (T)c.cfg.smootherWeight;
   const int inner = post ? c.cfg.postInnerIters : c.cfg.preInnerIters;
   if (smoother_in_registers(L.max_in_row, L.max_part_rows)) {
-    const int thr = ((L.max_group_rows + 31) / 32) * 32;
     auto k = post ? smooth_reg_kernel<T, true, kRegRow> : smooth_reg_kernel<T, false, kRegRow>;
-    FG_LAUNCH(k, L.ngroups, thr < 32 ? 32 : thr, 2 * (size_t)thr * sizeof(T), s, L.grows.p, L.Ain.rp.p,
-              L.Ain.ci.p, L.Ain.v.p, aorp, L.Aout.ci.p, L.Aout.v.p, L.diag.p, L.dinv.p, b, w, inner, xin, xout,
-              rout);
+    if (L.smooth_smem > 48 * 1024)
+      FG_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smooth_smem));
+    FG_LAUNCH(k, L.smooth_grid, L.smooth_threads, L.smooth_smem, s, L.ngroups, L.grows.p, L.Ain.rp.p, L.ci16.p,
+              L.Ain.v.p, L.diag.p, L.dinv.p, b, w, inner, xin, xout, rout, L.max_group_ents + 16,
+              c.red.p + 2 * kRedBlocks + S_KERR);
     return;
   }
-  const size_t sm = smooth_smem(L);
-  const bool st = staged(L);
-  const int S = smem_lanes(L.max_part_rows);
-  using KFn = void (*)(const int32_t*, const int32_t*, const int32_t*, const T*, const int32_t*, const int32_t*,
-                       const T*, const T*, const T*, const T*, T, int, const T*, T*, T*, int, int);
-  KFn k;
-#define FG_SMOOTH_PICK(SS)                                                                  \
-  k = post ? (st ? smooth_kernel<T, true, true, SS> : smooth_kernel<T, true, false, SS>)    \
-           : (st ? smooth_kernel<T, false, true, SS> : smooth_kernel<T, false, false, SS>)
-  switch (S) {
-    case 1: FG_SMOOTH_PICK(1); break;
-    case 2: FG_SMOOTH_PICK(2); break;
-    case 4: FG_SMOOTH_PICK(4); break;
-    case 8: FG_SMOOTH_PICK(8); break;
-    case 16: FG_SMOOTH_PICK(16); break;
-    default: FG_SMOOTH_PICK(32); break;
-  }
-#undef FG_SMOOTH_PICK
+  ClusterSmoothFn<T> k = pick_cluster_kernel<T>(post, L.smooth_staged, L.smooth_lanes);
   // the limit is a per-function attribute shared by every handle: set it per launch
-  if (sm > 48 * 1024) FG_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  FG_LAUNCH(k, L.ngroups, 1024, sm, s, L.grows.p, L.Ain.rp.p, L.Ain.ci.p, L.Ain.v.p, aorp,
-            L.Aout.ci.p, L.Aout.v.p, L.diag.p, L.dinv.p, b, w, inner, xin, xout, rout, L.max_part_rows,
-            L.max_part_entries);
+  if (L.smooth_smem > 48 * 1024)
+    FG_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smooth_smem));
+  launch_clustered(k, L.ngroups * L.cluster, L.smooth_threads, L.smooth_smem, L.cluster, s,
+                   (const int32_t*)L.grows.p, (const int32_t*)L.Ain.rp.p, (const int32_t*)L.Ain.ci.p,
+                   (const T*)L.Ain.v.p, aorp, (const int32_t*)L.Aout.ci.p, (const T*)L.Aout.v.p,
+                   (const T*)L.diag.p, (const T*)L.dinv.p, b, w, inner, xin, xout, rout, L.max_group_rows,
+                   L.slice_rows, L.slice_ents);
+}
+
+// Records a named event on the stream when stage timing is on (never during capture).
+void stage_mark(Ctx& c, const char* what, int l) {
+  if (!c.stage_marks) return;
+  cudaEvent_t e;
+  FG_CUDA(cudaEventCreate(&e));
+  FG_CUDA(cudaEventRecord(e, c.stream));
+  c.stage_marks->emplace_back(std::string(what) + " l" + std::to_string(l), e);
 }
 
 // b (level order for l > 0, already permuted for l == 0) -> x (same ordering).
@@ -563,32 +683,40 @@ void vcycle(Ctx& c, Hierarchy<T>& H, int l, const T* b_in, T* x_out) {
   const int n = L.A.n;
   if (L.coarsest) {
     FG_LAUNCH(coarse_solve_kernel<T>, grid_for((int64_t)n * 32, 256), 256, 0, s, n, L.Ainv.p, b_in, x_out);
+    stage_mark(c, "coarse", l);
     return;
   }
   const T* b = b_in;
   if (l > 0) {
     FG_LAUNCH(permute_in_kernel<T>, grid_for(n, 256), 256, 0, s, n, L.iperm.p, b_in, L.b.p);
     b = L.b.p;
+    stage_mark(c, "permute_in", l);
   }
   smooth<T>(c, L, false, b, nullptr, L.x.p, L.r.p);
+  stage_mark(c, "pre", l);
   FG_LAUNCH(aout_residual_kernel<T>, grid_for(n, 256), 256, 0, s, n, L.Aout.rp.p, L.Aout.ci.p, L.Aout.v.p, L.x.p,
             L.r.p);
+  stage_mark(c, "residual", l);
   // next level: input in its t (or b when coarsest), output in its xo (or x)
   Level<T>& N = *H.L[l + 1];
   T* bc = N.coarsest ? N.b.p : N.t.p;
   T* xc = N.coarsest ? N.x.p : N.xo.p;
   spmv_lanes(L.R, L.r.p, bc, 0, s);
+  stage_mark(c, "restrict", l);
   vcycle(c, H, l + 1, bc, xc);
   spmv_lanes(L.P, xc, L.x.p, 1, s);
+  stage_mark(c, "prolong", l);
   for (int rl = 0; rl < c.cfg.postRelaxes; rl++) {
     smooth<T>(c, L, true, b, L.x.p, L.r.p, nullptr);
     std::swap(L.x.p, L.r.p);  // r is free after the restriction: use it as the ping-pong buffer
   }
+  stage_mark(c, "post", l);
   if (l > 0) {
     FG_LAUNCH(permute_out_kernel<T>, grid_for(n, 256), 256, 0, s, n, L.iperm.p, L.x.p, x_out);
   } else {
     FG_CUDA(cudaMemcpyAsync(x_out, L.x.p, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
   }
+  stage_mark(c, "output", l);
 }
 
 // z = M r on permuted level-0 FP64 vectors.
@@ -600,8 +728,10 @@ void precondition(Ctx& c, Hierarchy<T>& H, const double* r, double* z) {
   T* b = L.coarsest ? L.b.p : L.t.p;
   T* x = L.coarsest ? L.x.p : L.xo.p;
   FG_LAUNCH(cast_in_kernel<T>, grid_for(n, 256), 256, 0, s, n, r, b);
+  stage_mark(c, "cast_in", 0);
   vcycle(c, H, 0, b, x);
   FG_LAUNCH(cast_out_kernel<T>, grid_for(n, 256), 256, 0, s, n, x, z);
+  stage_mark(c, "cast_out", 0);
 }
 
 void precondition_any(Ctx& c, const double* r, double* z) {
@@ -627,7 +757,91 @@ void ensure_work(Ctx& c, int n) {
   if (!c.h_scalars) FG_CUDA(cudaMallocHost((void**)&c.h_scalars, 64 * sizeof(double)));
 }
 
+// Fails when a smoother CTA gave up waiting for its bulk copies (waits on the stream).
+void check_kernel_error(Ctx& c) {
+  double v = 0.0;
+  FG_CUDA(cudaMemcpyAsync(&v, c.red.p + 2 * kRedBlocks + S_KERR, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+  FG_CUDA(cudaStreamSynchronize(c.stream));
+  FG_REQUIRE(v == 0.0, FEMGPU_ERR_LIMIT, "smoother copy wait ran out");
+}
+
 }  // namespace
+
+template <class T>
+void plan_smoother(Ctx& c, Level<T>& L) {
+  cudaStream_t s = c.stream;
+  if (smoother_in_registers(L.max_in_row, L.max_part_rows)) {
+    L.smooth_lanes = 1;
+    L.cluster = 1;
+    L.smooth_threads = std::max(32, ((L.max_group_rows + 31) / 32) * 32);
+    L.smooth_smem = reg_smem_layout<T>(L.max_group_ents + 16).total;
+    FG_REQUIRE(L.smooth_smem <= kSmemOptIn, FEMGPU_ERR_LIMIT, "register smoother staging exceeds shared memory");
+    int per_sm = 0;
+    for (int post = 0; post < 2; post++) {
+      auto k = post ? smooth_reg_kernel<T, true, kRegRow> : smooth_reg_kernel<T, false, kRegRow>;
+      if (L.smooth_smem > 48 * 1024)
+        FG_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smooth_smem));
+      int nb = 0;
+      FG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, L.smooth_threads, L.smooth_smem));
+      per_sm = post ? std::min(per_sm, nb) : nb;
+    }
+    FG_REQUIRE(per_sm > 0, FEMGPU_ERR_LIMIT, "no resident configuration for the register smoother");
+    int sms = 0;
+    FG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device));
+    L.smooth_grid = (int)std::min<int64_t>(L.ngroups, (int64_t)per_sm * sms);
+    return;
+  }
+  const int S = smooth_lanes_for(L.n, L.Ain.nnz);
+  const int mcap = L.max_group_rows;
+  L.smooth_lanes = S;
+  int C = (int)std::min<int64_t>(kMaxCluster, ((int64_t)mcap * S + 1023) / 1024);
+  if (C < 1) C = 1;
+  for (;; C--) {
+    DBuf<int32_t> sent((size_t)L.ngroups * C, s);
+    FG_LAUNCH(slice_entries_kernel, grid_for((int64_t)L.ngroups * C, 256), 256, 0, s, L.ngroups, C, L.grows.p,
+              L.Ain.rp.p, sent.p);
+    const int scap = (mcap + C - 1) / C;
+    const int ecap = reduce_max(sent.p, (int64_t)L.ngroups * C, s);
+    const bool st = mcap < 65536 && slice_smem_bytes<T>(mcap, scap, ecap) <= kStageLimit;
+    const size_t sm = slice_smem_bytes<T>(mcap, scap, st ? ecap : 0);
+    FG_REQUIRE(sm <= kSmemOptIn, FEMGPU_ERR_LIMIT, "partition too large for the shared-memory smoother");
+    const int64_t want = ((int64_t)scap * S + 31) / 32 * 32;
+    const int thr = (int)std::max<int64_t>(32, std::min<int64_t>(1024, want));
+    bool fits = true;
+    for (int post = 0; post < 2 && fits; post++) {
+      ClusterSmoothFn<T> k = pick_cluster_kernel<T>(post != 0, st, S);
+      if (sm > 48 * 1024) FG_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3((unsigned)(L.ngroups * C));
+      cfg.blockDim = dim3((unsigned)thr);
+      cfg.dynamicSmemBytes = sm;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = (unsigned)C;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      int clusters = 0;
+      const cudaError_t e = cudaOccupancyMaxActiveClusters(&clusters, k, &cfg);
+      if (e != cudaSuccess) (void)cudaGetLastError();
+      fits = e == cudaSuccess && clusters > 0;
+    }
+    if (fits || C == 1) {
+      FG_REQUIRE(fits, FEMGPU_ERR_LIMIT, "no resident configuration for the shared-memory smoother");
+      L.cluster = C;
+      L.slice_rows = scap;
+      L.slice_ents = ecap;
+      L.smooth_staged = st;
+      L.smooth_smem = sm;
+      L.smooth_threads = thr;
+      return;
+    }
+  }
+}
+
+template void plan_smoother<float>(Ctx&, Level<float>&);
+template void plan_smoother<double>(Ctx&, Level<double>&);
 
 void spmv_original(Ctx& c, const double* d_x, double* d_y) {
   FG_REQUIRE(c.has_matrix, FEMGPU_ERR_NOT_READY, "no operator");
@@ -640,9 +854,29 @@ void amg_vcycle_device(Ctx& c, const double* d_r, double* d_z) {
   const int n = c.A.n;
   cudaStream_t s = c.stream;
   ensure_work(c, n);
-  FG_LAUNCH(perm_vec_in_kernel, grid_for(n, 256), 256, 0, s, n, c.perm0.p, d_r, c.vr.p);
-  precondition_any(c, c.vr.p, c.vz.p);
-  FG_LAUNCH(perm_vec_out_kernel, grid_for(n, 256), 256, 0, s, n, c.perm0.p, c.vz.p, d_z);
+  std::vector<std::pair<std::string, cudaEvent_t>> marks;
+  if (getenv("FEMGPU_PROFILE")) c.stage_marks = &marks;
+  try {
+    FG_LAUNCH(perm_vec_in_kernel, grid_for(n, 256), 256, 0, s, n, c.perm0.p, d_r, c.vr.p);
+    stage_mark(c, "start", 0);
+    precondition_any(c, c.vr.p, c.vz.p);
+    FG_LAUNCH(perm_vec_out_kernel, grid_for(n, 256), 256, 0, s, n, c.perm0.p, c.vz.p, d_z);
+  } catch (...) {
+    c.stage_marks = nullptr;
+    for (auto& m : marks) cudaEventDestroy(m.second);
+    throw;
+  }
+  c.stage_marks = nullptr;
+  if (!marks.empty()) {
+    FG_CUDA(cudaEventSynchronize(marks.back().second));
+    for (size_t i = 1; i < marks.size(); i++) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, marks[i - 1].second, marks[i].second);
+      fprintf(stderr, "[femgpu vcycle] %-14s %8.1f us\n", marks[i].first.c_str(), ms * 1000.0f);
+    }
+    for (auto& m : marks) cudaEventDestroy(m.second);
+  }
+  check_kernel_error(c);
 }
 
 namespace {
@@ -752,6 +986,7 @@ SolveResult amg_solve_device(Ctx& c, const double* d_b, double* d_x) {
   FG_LAUNCH(finalize_kernel, 1, 1024, 0, s, part, kRedBlocks, sc + S_NR);
   FG_LAUNCH(set_slot_kernel, 1, 1, 0, s, sc, S_FLAG, 0.0);
   FG_LAUNCH(set_slot_kernel, 1, 1, 0, s, sc, S_FIRST, 1.0);
+  FG_LAUNCH(set_slot_kernel, 1, 1, 0, s, sc, S_KERR, 0.0);
   FG_CUDA(cudaMemsetAsync(c.vp.p, 0, n * sizeof(double), s));
   FG_CUDA(cudaMemcpyAsync(c.h_scalars, sc, S_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s));
   FG_CUDA(cudaStreamSynchronize(s));
@@ -775,6 +1010,7 @@ SolveResult amg_solve_device(Ctx& c, const double* d_b, double* d_x) {
       FG_CUDA(cudaStreamSynchronize(s));
       it++;
       nr = sqrt(c.h_scalars[S_NR]);
+      FG_REQUIRE(c.h_scalars[S_KERR] == 0.0, FEMGPU_ERR_LIMIT, "smoother copy wait ran out");
       if (c.h_scalars[S_FLAG] != 0.0 || !std::isfinite(nr)) {
         res.status = FEMGPU_ERR_BREAKDOWN;
         break;
@@ -845,6 +1081,7 @@ void profile_level0(Ctx& c, Hierarchy<T>& H, int which, int reps, double* ms, do
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   *ms = t / reps;
+  check_kernel_error(c);
 }
 
 }  // namespace

@@ -16,7 +16,15 @@ namespace {
 
 thread_local std::string g_last_global_error;
 
+// Routes the handle's allocations to its pool for the duration of one call.
+struct PoolScope {
+  cudaMemPool_t saved;
+  explicit PoolScope(femgpu_handle h) : saved(g_alloc_pool) { g_alloc_pool = h ? h->pool : nullptr; }
+  ~PoolScope() { g_alloc_pool = saved; }
+};
+
 femgpu_status guard(femgpu_handle h, const std::function<void()>& fn) {
+  PoolScope scope(h);
   try {
     if (h) FG_CUDA(cudaSetDevice(h->device));
     fn();
@@ -186,9 +194,25 @@ femgpu_status femgpu_create(femgpu_handle* out, const femgpu_config* cfg) {
       FG_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
       h->own_stream = true;
     }
+    if (h->cfg.mem_pool) {
+      h->pool = (cudaMemPool_t)h->cfg.mem_pool;
+    } else {
+      // freed memory stays in the pool for the next setup instead of going back to
+      // the driver at every synchronization
+      cudaMemPoolProps props = {};
+      props.allocType = cudaMemAllocationTypePinned;
+      props.location.type = cudaMemLocationTypeDevice;
+      props.location.id = h->device;
+      FG_CUDA(cudaMemPoolCreate(&h->pool, &props));
+      h->own_pool = true;
+      uint64_t keep = UINT64_MAX;
+      FG_CUDA(cudaMemPoolSetAttribute(h->pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    }
   });
   if (st != FEMGPU_OK) {
     g_last_global_error = h->last_error;
+    if (h->own_stream) cudaStreamDestroy(h->stream);
+    if (h->own_pool) cudaMemPoolDestroy(h->pool);
     delete h;
     return st;
   }
@@ -202,12 +226,12 @@ femgpu_status femgpu_destroy(femgpu_handle h) {
   cudaStreamSynchronize(h->stream);
   cudaStream_t s = h->stream;
   bool own = h->own_stream;
+  cudaMemPool_t pool = h->own_pool ? h->pool : nullptr;
   if (h->h_scalars) cudaFreeHost(h->h_scalars);
   delete h;  // buffers free asynchronously on s
-  if (own) {
-    cudaStreamSynchronize(s);
-    cudaStreamDestroy(s);
-  }
+  cudaStreamSynchronize(s);
+  if (own) cudaStreamDestroy(s);
+  if (pool) cudaMemPoolDestroy(pool);
   return FEMGPU_OK;
 }
 
@@ -223,6 +247,7 @@ femgpu_status femgpu_set_config(femgpu_handle h, const femgpu_config* cfg) {
     femgpu_config c = *cfg;
     c.device = h->cfg.device;
     c.stream = h->cfg.stream;
+    c.mem_pool = h->cfg.mem_pool;
     bool rebuild = c.precision != h->cfg.precision || c.seed != h->cfg.seed || c.maxLevels != h->cfg.maxLevels ||
                    c.topSize != h->cfg.topSize || c.randMisParameters != h->cfg.randMisParameters ||
                    c.partitionMaxSize != h->cfg.partitionMaxSize || c.proOmega != h->cfg.proOmega ||

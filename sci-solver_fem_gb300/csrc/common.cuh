@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <cstdio>
 #include <stdexcept>
 #include <string>
@@ -41,6 +42,10 @@ struct Error : std::runtime_error {
     if (!(cond)) throw ::femgpu::Error((status), (msg));  \
   } while (0)
 
+// Memory pool of the handle whose entry point is running on this thread (set by the
+// C ABI around each call); null = the device's current pool.
+extern thread_local cudaMemPool_t g_alloc_pool;
+
 // Stream-ordered device buffer.
 template <class T>
 struct DBuf {
@@ -66,7 +71,8 @@ struct DBuf {
     s = st;
     n = count;
     if (count) {
-      cudaError_t e = cudaMallocAsync((void**)&p, count * sizeof(T), st);
+      cudaError_t e = g_alloc_pool ? cudaMallocFromPoolAsync((void**)&p, count * sizeof(T), g_alloc_pool, st)
+                                   : cudaMallocAsync((void**)&p, count * sizeof(T), st);
       if (e != cudaSuccess) {
         p = nullptr;
         n = 0;
@@ -115,9 +121,13 @@ inline int grid_for(int64_t n, int block) {
   return (int)g;
 }
 
+// Host round trips of the setup (counted for its phase timer).
+extern std::atomic<int64_t> g_host_syncs;
+
 // Reads one device scalar synchronously (used only at setup-time loop checks).
 template <class T>
 inline T read_scalar(const T* d, cudaStream_t s) {
+  g_host_syncs.fetch_add(1, std::memory_order_relaxed);
   T h;
   FG_CUDA(cudaMemcpyAsync(&h, d, sizeof(T), cudaMemcpyDeviceToHost, s));
   FG_CUDA(cudaStreamSynchronize(s));
@@ -182,6 +192,49 @@ __host__ __device__ inline int next_pow2(int v) {
   int p = 1;
   while (p < v) p <<= 1;
   return p;
+}
+
+// ---- bulk asynchronous copies (TMA, 1-D) with an mbarrier -----------------------
+// cp.async.bulk moves a contiguous global range into shared memory; source,
+// destination and size must be multiples of 16 bytes.  Completion is counted in
+// bytes on an mbarrier in shared memory.
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// Waits for the barrier phase with an iteration limit; false when it ran out.
+constexpr int kMbarWaitLimit = 1 << 22;
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  for (int i = 0; i < kMbarWaitLimit; i++)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
 }
 
 }  // namespace femgpu

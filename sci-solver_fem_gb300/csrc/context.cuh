@@ -55,7 +55,15 @@ struct Level {
   int max_in_row = 0;        // longest in-partition row
   // smoother work groups: consecutive partitions packed per CTA (row offsets)
   DBuf<int32_t> grows;
-  int ngroups = 0, max_group_rows = 0;
+  int ngroups = 0, max_group_rows = 0, max_group_ents = 0;
+  // register smoother: in-partition columns relative to their group's first row
+  // (16 bit), padded by 16 entries like Ain.v so 16-byte rounded copies stay inside
+  DBuf<uint16_t> ci16;
+  // shared-memory smoother plan: lanes per row, CTAs per cluster (one cluster per
+  // group), rows and entries of the largest CTA row slice, launch shape
+  int smooth_lanes = 1, cluster = 1, slice_rows = 0, slice_ents = 0, smooth_threads = 0, smooth_grid = 0;
+  bool smooth_staged = false;
+  size_t smooth_smem = 0;
   // coarsest: explicit inverse, row-major n x n
   DBuf<double> Ainv;
   // work vectors (level numbering / permuted numbering)
@@ -68,6 +76,17 @@ constexpr int kRegRow = 16;
 constexpr int kRegGroupRows = 512;
 inline bool smoother_in_registers(int max_in_row, int max_part_rows) {
   return max_in_row <= kRegRow && max_part_rows <= kRegGroupRows;
+}
+
+// Lanes per row of the shared-memory smoother's in-partition sums (the CPU oracle
+// uses the same rule): doubled while every lane still adds at least 3 entries of an
+// average row and rows x lanes stay within one wave of 152 SMs x 2048 threads.
+constexpr int64_t kSmoothThreadBudget = 152LL * 2048;
+inline int smooth_lanes_for(int64_t rows, int64_t in_nnz) {
+  const int64_t avg = rows > 0 ? (in_nnz + rows - 1) / rows : 0;
+  int s = 1;
+  while (s < 32 && 3 * (2 * s) <= avg && rows * (2 * s) <= kSmoothThreadBudget) s <<= 1;
+  return s;
 }
 
 struct HierarchyBase {
@@ -85,6 +104,8 @@ struct Ctx {
   int device = 0;
   cudaStream_t stream = 0;
   bool own_stream = false;
+  cudaMemPool_t pool = nullptr;  // every device buffer of the handle comes from here
+  bool own_pool = false;
   std::string last_error;
 
   Mesh mesh;
@@ -110,6 +131,8 @@ struct Ctx {
   int graph_flexible = -1;
   cudaGraphExec_t pcg_exec = nullptr;
   int64_t graph_nodes = 0;
+  // stage timing of a V-cycle run outside capture (FEMGPU_PROFILE set): named events
+  std::vector<std::pair<std::string, cudaEvent_t>>* stage_marks = nullptr;
 
   ~Ctx() {
     if (pcg_exec) cudaGraphExecDestroy(pcg_exec);
@@ -135,6 +158,9 @@ struct SolveResult {
   femgpu_status status = FEMGPU_OK;
 };
 SolveResult amg_solve_device(Ctx& c, const double* d_b, double* d_x);
+// Chooses the smoother's launch plan for a level whose groups are built.
+template <class T>
+void plan_smoother(Ctx& c, Level<T>& L);
 void amg_vcycle_device(Ctx& c, const double* d_r, double* d_z);
 void spmv_original(Ctx& c, const double* d_x, double* d_y);
 void profile_kernel(Ctx& c, int which, int reps, double* ms, double* bytes);

@@ -40,6 +40,7 @@ class Config(C.Structure):
         ("solverType", C.c_int), ("smootherWeight", C.c_double), ("proOmega", C.c_double), ("device", C.c_int),
         ("blockSize", C.c_int), ("seed", C.c_uint32), ("precision", C.c_int), ("flexibleCG", C.c_int),
         ("stream", C.c_void_p),
+        ("mem_pool", C.c_void_p),
     ]
 
 
@@ -131,7 +132,7 @@ def kernel_launches() -> int:
 
 class Solver:
     """One solver context (femgpu_handle).  Keyword options are the FEMSolver members
-    (maxLevels, tolerance, solverType, ...) plus seed, precision, flexibleCG, stream."""
+    (maxLevels, tolerance, solverType, ...) plus seed, precision, flexibleCG, stream, mem_pool."""
 
     def __init__(self, **options):
         L = lib()

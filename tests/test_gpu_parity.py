@@ -121,9 +121,10 @@ def test_aggregates_bit_exact_across_seeds(seed):
         assert np.array_equal(go["part_idx"], oo["part_idx"])
 
 
-@pytest.mark.parametrize("precision", [0, 1])
-def test_vcycle_matches_oracle(precision):
-    orc, s, (rp, ci, v, b) = build_both(n=14, seed=5, precision=precision)
+@pytest.mark.parametrize("precision,n", [(0, 14), (1, 14), (0, 40), (1, 40)])
+def test_vcycle_matches_oracle(precision, n):
+    # n = 40: coarse levels run the shared-memory smoother on multi-CTA clusters
+    orc, s, (rp, ci, v, b) = build_both(n=n, seed=5, precision=precision, sigma=2.0)
     r = np.random.default_rng(0).standard_normal(rp.shape[0] - 1)
     zg, zo = s.vcycle(r), orc.vcycle(r)
     assert np.array_equal(zg, zo), np.abs(zg - zo).max() / np.abs(zo).max()

@@ -21,8 +21,8 @@ _USED_MEM_HIGH = 8
 
 
 class _StreamPool:
-    """Usage counters of the device's current memory pool (the pool cudaMallocAsync
-    draws from), read through the driver API."""
+    """Usage counters of the device's current memory pool, read through the driver
+    API; the solver under test is given this pool for its device buffers."""
 
     def __init__(self, device=0):
         self.cu = C.CDLL("libcuda.so.1")
@@ -47,14 +47,14 @@ class _StreamPool:
         assert self.cu.cuMemPoolSetAttribute(self.pool, _USED_MEM_HIGH, C.byref(zero)) == 0
 
 
-def _mesh_solver(kind):
+def _mesh_solver(kind, pool=None):
     rng = np.random.default_rng(11)
     if kind == "tet":
         xyz, conn = meshes.kuhn_cube(14)
         xyz = xyz + rng.uniform(-0.01, 0.01, xyz.shape)
     else:
         xyz, conn = meshes.jittered_square(40)
-    s = femgpu.Solver()
+    s = femgpu.Solver(mem_pool=pool.pool.value) if pool else femgpu.Solver()
     s.set_mesh(xyz, conn)
     return s, xyz.shape[0], rng
 
@@ -64,10 +64,16 @@ def test_two_consecutive_calls_match_allocating_entry_point(kind):
     import torch
 
     torch.cuda.init()
-    s, nv, rng = _mesh_solver(kind)
+    pool = _StreamPool()
+    s, nv, rng = _mesh_solver(kind, pool)
     f1 = rng.uniform(-1.0, 1.0, nv)
     f2 = rng.standard_normal(nv) * 3.0
+    torch.cuda.synchronize()
+    pool.reset_high()
+    before_alloc = pool.used()
     ref1 = s.load_vector(f1)
+    # the allocating entry point draws its buffers from this pool, so the pool sees them
+    assert pool.high() > before_alloc
     ref2 = s.load_vector(f2)
 
     dev = torch.device("cuda", 0)
@@ -77,7 +83,6 @@ def test_two_consecutive_calls_match_allocating_entry_point(kind):
     db2 = torch.full((nv,), float("nan"), dtype=torch.float64, device=dev)
     torch.cuda.synchronize()
 
-    pool = _StreamPool()
     used0 = pool.used()
     pool.reset_high()
     launches0 = femgpu.kernel_launches()
@@ -85,7 +90,7 @@ def test_two_consecutive_calls_match_allocating_entry_point(kind):
     s.load_vector_device_noalloc(df2.data_ptr(), db2.data_ptr())
     torch.cuda.synchronize()
     assert femgpu.kernel_launches() - launches0 == 4
-    # no stream-ordered allocation happened inside either call
+    # no allocation from the solver's pool happened inside either call
     assert pool.high() <= used0
     assert pool.used() == used0
 
