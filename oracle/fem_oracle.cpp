@@ -1144,6 +1144,8 @@ int setup_levels(orc_amg* h, std::vector<Level<T>>& L, const Csr<double>& A, con
       const int64_t avg = N > 0 ? (in_nnz + N - 1) / N : 0;
       int sl = 1;
       while (sl < 32 && 3 * (2 * sl) <= avg && (int64_t)N * (2 * sl) <= 152LL * 2048) sl <<= 1;
+      /* then while the longest row leaves a lane more than 16 entries */
+      while (sl < 32 && (max_row + sl - 1) / sl > 16) sl <<= 1;
       lv.smooth_lanes = (max_row <= 16 && max_part <= 512) ? 1 : sl;
     }
     lv.P = build_prolongator(lv.Ap, lv.diag, lv.aggOf, nagg, c.pro_omega);

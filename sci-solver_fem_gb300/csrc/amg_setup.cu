@@ -1724,7 +1724,10 @@ void build_levels(Ctx& c, Hierarchy<T>& H) {
         fprintf(stderr,
                 "[femgpu setup] level %d smoother: %s, groups %d (max %d rows), lanes %d, cluster %d, "
                 "slice %d rows / %d entries, %d threads, %zu B shared%s\n",
-                num_levels - 1, smoother_in_registers(L.max_in_row, L.max_part_rows) ? "registers" : "cluster",
+                num_levels - 1,
+                smoother_in_registers(L.max_in_row, L.max_part_rows) ? "registers"
+                : L.smooth_k > 0                                      ? "cluster, entries in registers"
+                                                                      : "cluster",
                 L.ngroups, L.max_group_rows, L.smooth_lanes, L.cluster, L.slice_rows, L.slice_ents,
                 L.smooth_threads, L.smooth_smem, L.smooth_staged ? ", staged" : "");
     }

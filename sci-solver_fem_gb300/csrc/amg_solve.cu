@@ -223,6 +223,95 @@ __global__ void __launch_bounds__(1024) smooth_cluster_kernel(
   }
 }
 
+// Cluster smoother with register-resident entries (groups split over a cluster as in
+// smooth_cluster_kernel): thread (t, j) of a CTA owns lane j of slice row t and keeps
+// that lane's entries j, j + S, ... (at most K, padded with zero values pointing at
+// the zero slot mcap of x) in registers across the sweeps, so a sweep is K
+// shared-memory loads and fused multiply-adds per lane, an xor butterfly, and the
+// broadcast of the row's new x to every CTA of the cluster.  Same order as
+// slice_row_sum.
+template <class T, bool POST, int S, int K>
+__global__ void __launch_bounds__(1024) smooth_creg_kernel(
+    const int32_t* __restrict__ grows, const int32_t* __restrict__ irp, const int32_t* __restrict__ ici,
+    const T* __restrict__ iv, const T* __restrict__ diag, const T* __restrict__ dinv, const T* __restrict__ b, T w,
+    int inner, const T* __restrict__ x_in, T* __restrict__ x_out, T* __restrict__ r_out, int mcap) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  T* const xa = reinterpret_cast<T*>(sm);
+  T* const xb = xa + (mcap + 1);
+  cg::cluster_group cl = cg::this_cluster();
+  const int C = (int)cl.num_blocks();
+  const int c = (int)cl.block_rank();
+  const int g = blockIdx.x / C;
+  const int rs = grows[g], m = grows[g + 1] - rs;
+  const int qs = (m + C - 1) / C;
+  const int ss = min(m, c * qs), ns = min(m, ss + qs) - ss;  // own slice: group rows [ss, ss + ns)
+  for (int t = threadIdx.x; t < m; t += blockDim.x) {
+    const int row = rs + t;
+    xa[t] = POST ? x_in[row] : (w * b[row]) * dinv[row];
+  }
+  if (threadIdx.x == 0) {
+    xa[mcap] = (T)0;
+    xb[mcap] = (T)0;
+  }
+  const int t = threadIdx.x / S, j = threadIdx.x & (S - 1);
+  const bool live = t < ns;
+  const int row = rs + ss + t;
+  int e0 = 0, len = 0;
+  T d = (T)1, di = (T)1, bb = (T)0, x = (T)0;
+  if (live) {
+    e0 = irp[row];
+    len = irp[row + 1] - e0;
+    d = diag[row];
+    di = dinv[row];
+    bb = b[row];
+    x = POST ? x_in[row] : (w * bb) * di;
+  }
+  T val[K];
+  uint32_t offp[K / 2];  // two 16-bit local columns per register
+#pragma unroll
+  for (int k = 0; k < K; k += 2) {
+    const int q0 = j + S * k, q1 = q0 + S;
+    const bool a0 = live && q0 < len, a1 = live && q1 < len;
+    val[k] = a0 ? iv[e0 + q0] : (T)0;
+    val[k + 1] = a1 ? iv[e0 + q1] : (T)0;
+    const uint32_t o0 = a0 ? (uint32_t)(ici[e0 + q0] - rs) : (uint32_t)mcap;
+    const uint32_t o1 = a1 ? (uint32_t)(ici[e0 + q1] - rs) : (uint32_t)mcap;
+    offp[k >> 1] = o0 | (o1 << 16);
+  }
+  cl.sync();  // every CTA of the cluster is running and holds x0
+  const T* cur = xa;
+  T* nxt = xb;
+  for (int it = 0; it < inner; it++) {
+    T sv = 0;
+#pragma unroll
+    for (int k = 0; k < K; k++) sv = fma(val[k], cur[(offp[k >> 1] >> ((k & 1) * 16)) & 0xffffu], sv);
+#pragma unroll
+    for (int off = S >> 1; off > 0; off >>= 1) sv = sv + __shfl_xor_sync(0xffffffffu, sv, off, S);
+    if (live && j == 0) {
+      x = relax(x, bb, sv, d, di, w);
+      for (int r = 0; r < C; r++) *cl.map_shared_rank(nxt + ss + t, r) = x;
+    }
+    cl.sync();  // all copies of the new x written; the old buffer is no longer read
+    T* tmp = const_cast<T*>(cur);
+    cur = nxt;
+    nxt = tmp;
+  }
+  if (!POST) {
+    T sv = 0;
+#pragma unroll
+    for (int k = 0; k < K; k++) sv = fma(val[k], cur[(offp[k >> 1] >> ((k & 1) * 16)) & 0xffffu], sv);
+#pragma unroll
+    for (int off = S >> 1; off > 0; off >>= 1) sv = sv + __shfl_xor_sync(0xffffffffu, sv, off, S);
+    if (live && j == 0) {
+      x_out[row] = x;
+      T u = bb - sv;
+      r_out[row] = u - d * x;
+    }
+  } else if (live && j == 0) {
+    x_out[row] = x;
+  }
+}
+
 // Shared memory of the register smoother: two mbarriers, x twice (kRegGroupRows + 1
 // slots each; the last slot stays 0 for padded entries), then two staging buffers for
 // a group's in-partition values and 16-bit local columns (ecap entries each, filled
@@ -376,14 +465,37 @@ __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
 }
 
 // r -= A_out x (preAout_kernel, gauss_seidel.cu:1977-2015).
+// Row sum s +/- v[q] x[ci[q]] over q = e, e + stride, ... < end, added in that order
+// with separately rounded products; the first K entries' columns, values and x are
+// all loaded before the first add, so a short row costs three dependent loads.
+template <class T, int K, bool SUB>
+__device__ __forceinline__ T gather_row(const int32_t* __restrict__ ci, const T* __restrict__ v,
+                                        const T* __restrict__ x, int e, int end, int stride, T s) {
+  int c[K];
+  T a[K], xv[K];
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    const int q = e + k * stride;
+    c[k] = q < end ? ci[q] : 0;
+    a[k] = q < end ? v[q] : (T)0;
+  }
+#pragma unroll
+  for (int k = 0; k < K; k++) xv[k] = e + k * stride < end ? x[c[k]] : (T)0;
+#pragma unroll
+  for (int k = 0; k < K; k++)
+    if (e + k * stride < end) s = SUB ? s - a[k] * xv[k] : s + a[k] * xv[k];
+  for (int q = e + K * stride; q < end; q += stride) s = SUB ? s - v[q] * x[ci[q]] : s + v[q] * x[ci[q]];
+  return s;
+}
+
 template <class T>
 __global__ void aout_residual_kernel(int n, const int32_t* __restrict__ orp, const int32_t* __restrict__ oci,
                                      const T* __restrict__ ov, const T* __restrict__ x, T* __restrict__ r) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  T s = 0;
-  for (int e = orp[i]; e < orp[i + 1]; e++) s = s + ov[e] * x[oci[e]];
-  r[i] = r[i] - s;
+  const T ri = r[i];
+  const T s = gather_row<T, 8, false>(oci, ov, x, orp[i], orp[i + 1], 1, (T)0);
+  r[i] = ri - s;
 }
 
 // y = M x (accumulate = 0) or y = y + M x (accumulate = 1) with S lanes per row:
@@ -396,8 +508,7 @@ __global__ void spmv_lanes_kernel(int n, const int32_t* __restrict__ rp, const i
   const int j = threadIdx.x & (S - 1);
   const bool live = g < n;
   T s = 0;
-  if (live)
-    for (int e = rp[g] + j; e < rp[g + 1]; e += S) s = s + v[e] * x[ci[e]];
+  if (live) s = gather_row<T, (S == 1 ? 8 : 4), false>(ci, v, x, rp[g] + j, rp[g + 1], S, (T)0);
 #pragma unroll
   for (int off = S >> 1; off > 0; off >>= 1) s = s + __shfl_xor_sync(0xffffffffu, s, off, S);
   if (live && j == 0) y[g] = accumulate ? y[g] + s : s;
@@ -589,6 +700,28 @@ ClusterSmoothFn<T> pick_cluster_kernel(bool post, bool staged, int S) {
 #undef FG_SMOOTH_PICK
 }
 
+template <class T>
+using CregSmoothFn = void (*)(const int32_t*, const int32_t*, const int32_t*, const T*, const T*, const T*, const T*,
+                              T, int, const T*, T*, T*, int);
+
+template <class T, int S>
+CregSmoothFn<T> pick_creg_k(bool post, int K) {
+  if (K <= 8) return post ? smooth_creg_kernel<T, true, S, 8> : smooth_creg_kernel<T, false, S, 8>;
+  return post ? smooth_creg_kernel<T, true, S, 16> : smooth_creg_kernel<T, false, S, 16>;
+}
+
+template <class T>
+CregSmoothFn<T> pick_creg_kernel(bool post, int S, int K) {
+  switch (S) {
+    case 1: return pick_creg_k<T, 1>(post, K);
+    case 2: return pick_creg_k<T, 2>(post, K);
+    case 4: return pick_creg_k<T, 4>(post, K);
+    case 8: return pick_creg_k<T, 8>(post, K);
+    case 16: return pick_creg_k<T, 16>(post, K);
+    default: return pick_creg_k<T, 32>(post, K);
+  }
+}
+
 // Launch with a 1-D thread-block cluster of `cluster` CTAs (counted like FG_LAUNCH).
 template <class... KArgs, class... Args>
 void launch_clustered(void (*k)(KArgs...), int grid, int block, size_t smem, int cluster, cudaStream_t s,
@@ -628,9 +761,8 @@ __global__ void aout_rhs_kernel(int n, const int32_t* __restrict__ orp, const in
                                 T* __restrict__ bp) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  T acc = b[i];
-  for (int e = orp[i]; e < orp[i + 1]; e++) acc = acc + (-ov[e]) * x[oci[e]];
-  bp[i] = acc;
+  // acc + (-v) x and acc - v x round identically: the negation is exact
+  bp[i] = gather_row<T, 8, true>(oci, ov, x, orp[i], orp[i + 1], 1, b[i]);
 }
 
 // Post relaxes take b' from aout_rhs_kernel (orp == nullptr inside the smoother).
@@ -653,6 +785,16 @@ void smooth(Ctx& c, Level<T>& L, bool post, const T* b, const T* xin, T* xout, T
     FG_LAUNCH(k, L.smooth_grid, L.smooth_threads, L.smooth_smem, s, L.ngroups, L.grows.p, L.Ain.rp.p, L.ci16.p,
               L.Ain.v.p, L.diag.p, L.dinv.p, b, w, inner, xin, xout, rout, L.max_group_ents + 16,
               c.red.p + 2 * kRedBlocks + S_KERR);
+    return;
+  }
+  if (L.smooth_k > 0) {
+    CregSmoothFn<T> k = pick_creg_kernel<T>(post, L.smooth_lanes, L.smooth_k);
+    if (L.smooth_smem > 48 * 1024)
+      FG_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smooth_smem));
+    launch_clustered(k, L.ngroups * L.cluster, L.smooth_threads, L.smooth_smem, L.cluster, s,
+                     (const int32_t*)L.grows.p, (const int32_t*)L.Ain.rp.p, (const int32_t*)L.Ain.ci.p,
+                     (const T*)L.Ain.v.p, (const T*)L.diag.p, (const T*)L.dinv.p, b, w, inner, xin, xout, rout,
+                     L.max_group_rows);
     return;
   }
   ClusterSmoothFn<T> k = pick_cluster_kernel<T>(post, L.smooth_staged, L.smooth_lanes);
@@ -791,9 +933,53 @@ void plan_smoother(Ctx& c, Level<T>& L) {
     L.smooth_grid = (int)std::min<int64_t>(L.ngroups, (int64_t)per_sm * sms);
     return;
   }
-  const int S = smooth_lanes_for(L.n, L.Ain.nnz);
+  const int S = smooth_lanes_for(L.n, L.Ain.nnz, L.max_in_row);
   const int mcap = L.max_group_rows;
   L.smooth_lanes = S;
+  L.smooth_k = 0;
+  // register-resident entries: at most 16 per lane, one row slice per CTA of <= 1024
+  // threads, 16-bit group-local columns
+  const int per_lane = (L.max_in_row + S - 1) / S;
+  const int rows_per_cta = 1024 / S;
+  const int creg_c = (mcap + rows_per_cta - 1) / rows_per_cta;
+  if (per_lane <= kLaneEntries && creg_c <= kMaxCluster && mcap < 65535) {
+    const int K = per_lane <= 8 ? 8 : 16;
+    for (int C = std::max(1, creg_c); C <= kMaxCluster; C++) {
+      const int scap = (mcap + C - 1) / C;
+      const int thr = (int)std::max<int64_t>(32, ((int64_t)scap * S + 31) / 32 * 32);
+      const size_t sm = 2 * (size_t)(mcap + 1) * sizeof(T);
+      bool fits = true;
+      for (int post = 0; post < 2 && fits; post++) {
+        CregSmoothFn<T> k = pick_creg_kernel<T>(post != 0, S, K);
+        if (sm > 48 * 1024) FG_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)(L.ngroups * C));
+        cfg.blockDim = dim3((unsigned)thr);
+        cfg.dynamicSmemBytes = sm;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = (unsigned)C;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int clusters = 0;
+        const cudaError_t e = cudaOccupancyMaxActiveClusters(&clusters, k, &cfg);
+        if (e != cudaSuccess) (void)cudaGetLastError();
+        fits = e == cudaSuccess && clusters > 0;
+      }
+      if (fits) {
+        L.smooth_k = K;
+        L.cluster = C;
+        L.slice_rows = scap;
+        L.slice_ents = 0;
+        L.smooth_staged = false;
+        L.smooth_smem = sm;
+        L.smooth_threads = thr;
+        return;
+      }
+    }
+  }
   int C = (int)std::min<int64_t>(kMaxCluster, ((int64_t)mcap * S + 1023) / 1024);
   if (C < 1) C = 1;
   for (;; C--) {

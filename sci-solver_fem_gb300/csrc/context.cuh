@@ -62,6 +62,7 @@ struct Level {
   // shared-memory smoother plan: lanes per row, CTAs per cluster (one cluster per
   // group), rows and entries of the largest CTA row slice, launch shape
   int smooth_lanes = 1, cluster = 1, slice_rows = 0, slice_ents = 0, smooth_threads = 0, smooth_grid = 0;
+  int smooth_k = 0;  // entries per lane of the register-resident cluster smoother (0: not used)
   bool smooth_staged = false;
   size_t smooth_smem = 0;
   // coarsest: explicit inverse, row-major n x n
@@ -80,12 +81,15 @@ inline bool smoother_in_registers(int max_in_row, int max_part_rows) {
 
 // Lanes per row of the shared-memory smoother's in-partition sums (the CPU oracle
 // uses the same rule): doubled while every lane still adds at least 3 entries of an
-// average row and rows x lanes stay within one wave of 152 SMs x 2048 threads.
+// average row and rows x lanes stay within one wave of 152 SMs x 2048 threads, then
+// while the longest row leaves a lane more than 16 entries (so they fit registers).
 constexpr int64_t kSmoothThreadBudget = 152LL * 2048;
-inline int smooth_lanes_for(int64_t rows, int64_t in_nnz) {
+constexpr int kLaneEntries = 16;
+inline int smooth_lanes_for(int64_t rows, int64_t in_nnz, int max_row) {
   const int64_t avg = rows > 0 ? (in_nnz + rows - 1) / rows : 0;
   int s = 1;
   while (s < 32 && 3 * (2 * s) <= avg && rows * (2 * s) <= kSmoothThreadBudget) s <<= 1;
+  while (s < 32 && (max_row + s - 1) / s > kLaneEntries) s <<= 1;
   return s;
 }
 
