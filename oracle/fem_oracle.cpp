@@ -1050,9 +1050,11 @@ void dense_solve(int n, const std::vector<double>& F, const std::vector<int32_t>
     for (int j = 0; j < i; j++) s = fma(-F[(size_t)i * n + j], b[j], s);
     b[i] = s;
   }
+  /* back substitution column by column (the device's order): row i takes the
+   * updates of columns n-1, n-2, ..., i+1, then the division */
   for (int i = n - 1; i >= 0; i--) {
     double s = b[i];
-    for (int j = i + 1; j < n; j++) s = fma(-F[(size_t)i * n + j], b[j], s);
+    for (int j = n - 1; j > i; j--) s = fma(-F[(size_t)i * n + j], b[j], s);
     b[i] = s / F[(size_t)i * n + i];
   }
 }

@@ -1527,28 +1527,97 @@ __global__ void dense_lu_kernel(int n, double* F, int32_t* piv, int32_t* status)
   }
 }
 
-// Column j of the inverse: solve LU x = P e_j with the factor (one thread per column).
-__global__ void dense_inverse_kernel(int n, const double* F, const int32_t* piv, double* work, double* inv) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= n) return;
-  double* b = work + (int64_t)j * n;
-  for (int i = 0; i < n; i++) b[i] = (i == j) ? 1.0 : 0.0;
+// The same factorization with the matrix in shared memory (n * n doubles), one block:
+// warp 0 finds the pivot (first maximal |a| in row order), every thread then swaps,
+// scales and updates the trailing block.  Identical arithmetic to dense_lu_kernel.
+__global__ void __launch_bounds__(1024) dense_lu_smem_kernel(int n, double* F, int32_t* piv, int32_t* status) {
+  extern __shared__ double sf[];
+  __shared__ int s_p;
+  __shared__ double s_pb;
+  for (int q = threadIdx.x; q < n * n; q += blockDim.x) sf[q] = F[q];
+  __syncthreads();
   for (int k = 0; k < n; k++) {
-    double t = b[k];
-    b[k] = b[piv[k]];
-    b[piv[k]] = t;
+    if (threadIdx.x < 32) {
+      double best = -1.0;
+      int bi = n;
+      for (int i = k + (int)threadIdx.x; i < n; i += 32) {
+        const double a = fabs(sf[i * n + k]);
+        if (a > best) {  // rows visited in ascending order per lane
+          best = a;
+          bi = i;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi < bi)) {
+          best = ob;
+          bi = oi;
+        }
+      }
+      if (threadIdx.x == 0) {
+        s_p = bi;
+        s_pb = best;
+      }
+    }
+    __syncthreads();
+    const int p = s_p;
+    if (s_pb == 0.0) {
+      if (threadIdx.x == 0) *status = 1;
+      return;
+    }
+    if (threadIdx.x == 0) piv[k] = p;
+    if (p != k)
+      for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        const double t = sf[k * n + j];
+        sf[k * n + j] = sf[p * n + j];
+        sf[p * n + j] = t;
+      }
+    __syncthreads();
+    const double d = sf[k * n + k];
+    for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) sf[i * n + k] = sf[i * n + k] / d;
+    __syncthreads();
+    const int m = n - k - 1;
+    for (int q = threadIdx.x; q < m * m; q += blockDim.x) {
+      const int i = k + 1 + q / m, j = k + 1 + q % m;
+      sf[i * n + j] = fma(-sf[i * n + k], sf[k * n + j], sf[i * n + j]);
+    }
+    __syncthreads();
   }
-  for (int i = 0; i < n; i++) {
-    double s = b[i];
-    for (int q = 0; q < i; q++) s = fma(-F[(int64_t)i * n + q], b[q], s);
-    b[i] = s;
+  for (int q = threadIdx.x; q < n * n; q += blockDim.x) F[q] = sf[q];
+}
+
+// Column j of the inverse (block j): solve L U x = P e_j column by column, so each
+// step updates every remaining row in parallel.  Forward: row i takes the updates of
+// columns 0, 1, ..., i-1 in that order; back: columns n-1, ..., i+1, then the division
+// by U_ii (the CPU oracle uses the same orders).
+__global__ void dense_inverse_kernel(int n, const double* __restrict__ F, const int32_t* __restrict__ piv,
+                                     double* __restrict__ inv) {
+  extern __shared__ double sb[];
+  const int j = blockIdx.x;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) sb[i] = (i == j) ? 1.0 : 0.0;
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int k = 0; k < n; k++) {
+      const double t = sb[k];
+      sb[k] = sb[piv[k]];
+      sb[piv[k]] = t;
+    }
+  __syncthreads();
+  for (int q = 0; q < n; q++) {
+    const double bq = sb[q];
+    for (int i = q + 1 + threadIdx.x; i < n; i += blockDim.x) sb[i] = fma(-F[(int64_t)i * n + q], bq, sb[i]);
+    __syncthreads();
   }
-  for (int i = n - 1; i >= 0; i--) {
-    double s = b[i];
-    for (int q = i + 1; q < n; q++) s = fma(-F[(int64_t)i * n + q], b[q], s);
-    b[i] = s / F[(int64_t)i * n + i];
+  for (int q = n - 1; q >= 0; q--) {
+    if (threadIdx.x == 0) sb[q] = sb[q] / F[(int64_t)q * n + q];
+    __syncthreads();
+    const double bq = sb[q];
+    for (int i = threadIdx.x; i < q; i += blockDim.x) sb[i] = fma(-F[(int64_t)i * n + q], bq, sb[i]);
+    __syncthreads();
   }
-  for (int i = 0; i < n; i++) inv[(int64_t)i * n + j] = b[i];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) inv[(int64_t)i * n + j] = sb[i];
 }
 
 __global__ void partition_rows_kernel(int npart, const int32_t* part_idx, const int32_t* agg_idx, int32_t* rows) {
@@ -1644,15 +1713,26 @@ void build_levels(Ctx& c, Hierarchy<T>& H) {
     if (N < c.cfg.topSize || num_levels >= c.cfg.maxLevels) {
       FG_REQUIRE(N <= 8192, FEMGPU_ERR_LIMIT, "coarsest level too large for the dense solve (raise maxLevels)");
       L.coarsest = true;
-      DBuf<double> F((size_t)N * N, s), work((size_t)N * N, s);
+      DBuf<double> F((size_t)N * N, s);
       DBuf<int32_t> piv(N, s), st(1, s);
       F.zero();
       st.zero();
       FG_LAUNCH(densify_kernel<T>, grid_for(N, 128), 128, 0, s, N, L.A.rp.p, L.A.ci.p, L.A.v.p, F.p);
-      FG_LAUNCH(dense_lu_kernel, 1, 1024, 0, s, N, F.p, piv.p, st.p);
+      const size_t fbytes = (size_t)N * N * sizeof(double);
+      if (fbytes <= 200 * 1024) {
+        if (fbytes > 48 * 1024)
+          FG_CUDA(cudaFuncSetAttribute(dense_lu_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fbytes));
+        FG_LAUNCH(dense_lu_smem_kernel, 1, 1024, fbytes, s, N, F.p, piv.p, st.p);
+      } else {
+        FG_LAUNCH(dense_lu_kernel, 1, 1024, 0, s, N, F.p, piv.p, st.p);
+      }
       FG_REQUIRE(read_scalar(st.p, s) == 0, FEMGPU_ERR_BREAKDOWN, "coarsest matrix is singular");
       L.Ainv.alloc((size_t)N * N, s);
-      FG_LAUNCH(dense_inverse_kernel, grid_for(N, 64), 64, 0, s, N, F.p, piv.p, work.p, L.Ainv.p);
+      const size_t bbytes = (size_t)N * sizeof(double);
+      if (bbytes > 48 * 1024)
+        FG_CUDA(cudaFuncSetAttribute(dense_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bbytes));
+      FG_LAUNCH(dense_inverse_kernel, N, std::min(1024, std::max(32, (N + 31) / 32 * 32)), bbytes, s, N, F.p, piv.p,
+                L.Ainv.p);
       L.b.alloc(N, s);
       L.x.alloc(N, s);
       break;
@@ -1817,6 +1897,21 @@ std::atomic<int64_t> g_kernel_launches{0};
 std::atomic<int64_t> g_host_syncs{0};
 thread_local cudaMemPool_t g_alloc_pool = nullptr;
 
+// Values of perm(A) on its (sorted) pattern: row i' and column j' of the permuted
+// matrix are row iperm[i'] and column iperm[j'] of A, found by binary search.
+__global__ void permuted_values_kernel(int n, const int32_t* __restrict__ prp, const int32_t* __restrict__ pci,
+                                       const int32_t* __restrict__ iperm, const int32_t* __restrict__ arp,
+                                       const int32_t* __restrict__ aci, const double* __restrict__ av,
+                                       double* __restrict__ pv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int r = iperm[i], a0 = arp[r], a1 = arp[r + 1];
+  for (int e = prp[i]; e < prp[i + 1]; e++) {
+    const int q = lower_bound_i32(aci, a0, a1, iperm[pci[e]]);
+    pv[e] = av[q];
+  }
+}
+
 void amg_setup(Ctx& c) {
   cudaStream_t s = c.stream;
   FG_REQUIRE(c.has_matrix, FEMGPU_ERR_NOT_READY, "no operator: call femgpu_set_mesh + femgpu_assemble or femgpu_set_matrix_csr");
@@ -1845,17 +1940,34 @@ void amg_setup(Ctx& c) {
     FG_CUDA(cudaMemcpyAsync(c.perm0.p, perm0, n * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
   else
     FG_LAUNCH(identity_kernel, grid_for(n, 256), 256, 0, s, n, c.perm0.p);
-  // FP64 outer operator in level-0 order
+  // FP64 outer operator in level-0 order: the pattern of the level-0 permuted operator
+  // (already built, rows sorted by column), values looked up in the FP64 matrix
   {
     DBuf<int32_t> iperm(n, s);
     FG_LAUNCH(invert_kernel, grid_for(n, 256), 256, 0, s, n, c.perm0.p, iperm.p);
-    EscArgs<double> a{};
-    a.arp = c.A.rp.p;
-    a.aci = c.A.ci.p;
-    a.av = c.A.v.p;
-    a.perm = c.perm0.p;
-    a.iperm = iperm.p;
-    run_esc<double, ESC_PERMUTE>(c, a, n, n, c.A0p);
+    const int32_t *prp, *pci;
+    int64_t pnnz;
+    if (c.cfg.precision == 1) {
+      const Level<double>& L0 = *static_cast<Hierarchy<double>&>(*c.H).L[0];
+      prp = L0.coarsest ? c.A.rp.p : L0.Ap.rp.p;
+      pci = L0.coarsest ? c.A.ci.p : L0.Ap.ci.p;
+      pnnz = L0.coarsest ? c.A.nnz : L0.Ap.nnz;
+    } else {
+      const Level<float>& L0 = *static_cast<Hierarchy<float>&>(*c.H).L[0];
+      prp = L0.coarsest ? c.A.rp.p : L0.Ap.rp.p;
+      pci = L0.coarsest ? c.A.ci.p : L0.Ap.ci.p;
+      pnnz = L0.coarsest ? c.A.nnz : L0.Ap.nnz;
+    }
+    c.A0p.n = c.A0p.m = n;
+    c.A0p.nnz = pnnz;
+    c.A0p.rp.alloc(n + 1, s);
+    c.A0p.ci.alloc(pnnz > 0 ? pnnz : 1, s);
+    c.A0p.v.alloc(pnnz > 0 ? pnnz : 1, s);
+    FG_CUDA(cudaMemcpyAsync(c.A0p.rp.p, prp, (n + 1) * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
+    if (pnnz > 0)
+      FG_CUDA(cudaMemcpyAsync(c.A0p.ci.p, pci, pnnz * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
+    FG_LAUNCH(permuted_values_kernel, grid_for(n, 128), 128, 0, s, n, c.A0p.rp.p, c.A0p.ci.p, iperm.p, c.A.rp.p,
+              c.A.ci.p, c.A.v.p, c.A0p.v.p);
   }
   FG_CUDA(cudaEventRecord(e1, s));
   FG_CUDA(cudaEventSynchronize(e1));
