@@ -1250,16 +1250,84 @@ __device__ bool hash_row_accumulate_matched(const EscArgs<T>& a, int i, int32_t*
   return *s_flag == 0;
 }
 
+// Galerkin-product rows with few distinct columns: one thread per row keeps up to
+// kRowSlots (column, value) pairs in shared memory and adds every product to its
+// column's slot in generation order (entries of the left row in order, each times
+// the right row in order), the first product of a column starting its slot; rows
+// with more distinct columns are listed for the warp tier.  Same sums as the hash
+// tiers, sorted by column on output.
+constexpr int kRowSlots = 32;
+constexpr int kRowThreads = 128;
+
 template <class T>
-__global__ void hash_warp_kernel(EscArgs<T> a, const int32_t* toff, int32_t* tci, T* tv, int32_t* counts,
-                                 int32_t* over, int32_t* nover) {
+__global__ void __launch_bounds__(kRowThreads) spgemm_row_kernel(EscArgs<T> a, const int32_t* toff, int32_t* tci,
+                                                                 T* tv, int32_t* counts, int32_t* over,
+                                                                 int32_t* nover) {
+  __shared__ int32_t sc[kRowSlots][kRowThreads];
+  __shared__ T sv[kRowSlots][kRowThreads];
+  const int t = threadIdx.x;
+  const int i = blockIdx.x * blockDim.x + t;
+  if (i >= a.n) return;
+  int u = 0;
+  bool overflow = false;
+  for (int e = a.arp[i]; e < a.arp[i + 1] && !overflow; e++) {
+    const int k = a.aci[e];
+    const T av = a.av[e];
+    for (int f = a.brp[k]; f < a.brp[k + 1]; f++) {
+      const int j = a.bci[f];
+      const T p = av * a.bv[f];
+      int q = 0;
+      while (q < u && sc[q][t] != j) q++;
+      if (q < u) {
+        sv[q][t] = sv[q][t] + p;
+      } else if (u < kRowSlots) {
+        sc[u][t] = j;
+        sv[u][t] = p;
+        u++;
+      } else {
+        overflow = true;
+        break;
+      }
+    }
+  }
+  if (overflow) {
+    over[atomicAdd(nover, 1)] = i;
+    counts[i] = 0;
+    return;
+  }
+  for (int q = 1; q < u; q++) {
+    const int cj = sc[q][t];
+    const T vj = sv[q][t];
+    int p = q - 1;
+    while (p >= 0 && sc[p][t] > cj) {
+      sc[p + 1][t] = sc[p][t];
+      sv[p + 1][t] = sv[p][t];
+      p--;
+    }
+    sc[p + 1][t] = cj;
+    sv[p + 1][t] = vj;
+  }
+  const int o = toff[i];
+  for (int q = 0; q < u; q++) {
+    tci[o + q] = sc[q][t];
+    tv[o + q] = sv[q][t];
+  }
+  counts[i] = u;
+}
+
+// Rows `rows[0 .. *nrows)` (all rows when rows == nullptr), one warp per row.
+template <class T>
+__global__ void hash_warp_kernel(EscArgs<T> a, const int32_t* rows, const int32_t* nrows, const int32_t* toff,
+                                 int32_t* tci, T* tv, int32_t* counts, int32_t* over, int32_t* nover) {
   __shared__ int32_t hk[kHashWarps][kHashWarpCap];
   __shared__ T hv[kHashWarps][kHashWarpCap];
   __shared__ unsigned long long lst[kHashWarps][kHashWarpCap];
   __shared__ T sv[kHashWarps][32];
   __shared__ int s_flag[kHashWarps];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int i = blockIdx.x * kHashWarps + w; i < a.n; i += gridDim.x * kHashWarps) {
+  const int nr = rows ? *nrows : a.n;
+  for (int ii = blockIdx.x * kHashWarps + w; ii < nr; ii += gridDim.x * kHashWarps) {
+    const int i = rows ? rows[ii] : ii;
     bool ok = hash_row_accumulate_matched<T>(a, i, hk[w], hv[w], sv[w], kHashWarpCap, lane, &s_flag[w]);
     if (!ok) {
       if (lane == 0) {
@@ -1324,6 +1392,7 @@ __global__ void compact_rows_copy_kernel(int n, const int32_t* toff, const int32
 template <class T>
 void run_spgemm_hash(Ctx& c, EscArgs<T> a, int nrows_out, int ncols_out, DCsr<T>& out) {
   cudaStream_t s = c.stream;
+  PhaseTimer pt(s, -2);
   a.n = nrows_out;
   DBuf<int32_t> items(nrows_out + 1, s), capv(nrows_out + 1, s), toff(nrows_out + 1, s), cnt(nrows_out + 1, s);
   a.counts = items.p;
@@ -1333,11 +1402,24 @@ void run_spgemm_hash(Ctx& c, EscArgs<T> a, int nrows_out, int ncols_out, DCsr<T>
   FG_REQUIRE(tcap < INT32_MAX, FEMGPU_ERR_LIMIT, "SpGEMM temporary exceeds int32 indexing");
   DBuf<int32_t> tci(tcap > 0 ? tcap : 1, s);
   DBuf<T> tv(tcap > 0 ? tcap : 1, s);
+  pt.mark("sp items");
   DBuf<int32_t> over1(nrows_out + 1, s), nover1(1, s), over2(nrows_out + 1, s), nover2(1, s);
   nover1.zero();
   nover2.zero();
   const int wgrid = std::min<int64_t>((nrows_out + kHashWarps - 1) / kHashWarps, 152 * 32);
-  FG_LAUNCH(hash_warp_kernel<T>, wgrid, 32 * kHashWarps, 0, s, a, toff.p, tci.p, tv.p, cnt.p, over1.p, nover1.p);
+  if (nrows_out >= 65536 && tcap <= (int64_t)nrows_out * 128) {
+    // short rows on average: thread-per-row tier first, its overflow rows to the warp tier
+    DBuf<int32_t> over0(nrows_out + 1, s), nover0(1, s);
+    nover0.zero();
+    FG_LAUNCH(spgemm_row_kernel<T>, grid_for(nrows_out, kRowThreads), kRowThreads, 0, s, a, toff.p, tci.p, tv.p,
+              cnt.p, over0.p, nover0.p);
+    FG_LAUNCH(hash_warp_kernel<T>, wgrid, 32 * kHashWarps, 0, s, a, over0.p, nover0.p, toff.p, tci.p, tv.p, cnt.p,
+              over1.p, nover1.p);
+  } else {
+    FG_LAUNCH(hash_warp_kernel<T>, wgrid, 32 * kHashWarps, 0, s, a, (const int32_t*)nullptr,
+              (const int32_t*)nullptr, toff.p, tci.p, tv.p, cnt.p, over1.p, nover1.p);
+  }
+  pt.mark("sp rows");
   const int n1 = read_scalar(nover1.p, s);
   if (n1 > 0) {
     const size_t bsm = (size_t)kHashBlockCap * (sizeof(unsigned long long) + sizeof(T) + sizeof(int32_t));
@@ -1366,6 +1448,7 @@ void run_spgemm_hash(Ctx& c, EscArgs<T> a, int nrows_out, int ncols_out, DCsr<T>
                 nullptr);
     }
   }
+  pt.mark("sp big");
   out.n = nrows_out;
   out.m = ncols_out;
   out.rp.alloc(nrows_out + 1, s);
@@ -1374,6 +1457,7 @@ void run_spgemm_hash(Ctx& c, EscArgs<T> a, int nrows_out, int ncols_out, DCsr<T>
   out.v.alloc(out.nnz > 0 ? out.nnz : 1, s);
   FG_LAUNCH(compact_rows_copy_kernel<T>, grid_for((int64_t)nrows_out * 32, 256), 256, 0, s, nrows_out, toff.p, tci.p,
             tv.p, out.rp.p, out.ci.p, out.v.p);
+  pt.mark("sp out");
 }
 
 template <class T, int MODE>
