@@ -30,7 +30,8 @@ constexpr int kRedThreads = 256;
 
 // device scalar slots in Ctx::red (after the partials)
 enum Slot {
-  S_BN = 0, S_NR, S_YP, S_ALPHA, S_RZ, S_RZNEW, S_ZROLD, S_BETA, S_FLAG, S_FIRST, S_KERR, S_COUNT
+  S_BN = 0, S_NR, S_YP, S_ALPHA, S_RZ, S_RZNEW, S_ZROLD, S_BETA, S_FLAG, S_FIRST, S_KERR,
+  S_IT, S_BNORM, S_TOL, S_MAXIT, S_COUNT
 };
 
 __device__ __forceinline__ double block_sum(double v, double* sh) {
@@ -157,7 +158,7 @@ __global__ void __launch_bounds__(1024) smooth_cluster_kernel(
     const int32_t* __restrict__ oci, const T* __restrict__ ov, const T* __restrict__ diag,
     const T* __restrict__ dinv, const T* __restrict__ b, T w, int inner, const T* __restrict__ x_in,
     T* __restrict__ x_out, T* __restrict__ r_out, int mcap, int scap, int ecap) {
-  extern __shared__ __align__(16) unsigned char sm[];
+  extern __shared__ __align__(128) unsigned char sm[];
   cg::cluster_group cl = cg::this_cluster();
   const int C = (int)cl.num_blocks();
   const int c = (int)cl.block_rank();
@@ -235,7 +236,7 @@ __global__ void __launch_bounds__(1024) smooth_creg_kernel(
     const int32_t* __restrict__ grows, const int32_t* __restrict__ irp, const int32_t* __restrict__ ici,
     const T* __restrict__ iv, const T* __restrict__ diag, const T* __restrict__ dinv, const T* __restrict__ b, T w,
     int inner, const T* __restrict__ x_in, T* __restrict__ x_out, T* __restrict__ r_out, int mcap) {
-  extern __shared__ __align__(16) unsigned char sm[];
+  extern __shared__ __align__(128) unsigned char sm[];
   T* const xa = reinterpret_cast<T*>(sm);
   T* const xb = xa + (mcap + 1);
   cg::cluster_group cl = cg::this_cluster();
@@ -530,21 +531,6 @@ __global__ void coarse_solve_kernel(int n, const double* __restrict__ inv, const
 
 // ---- FP64 PCG kernels -----------------------------------------------------------------
 // y = A p (rows in order, fused multiply-add) and a partial dot(y, p).
-__global__ void spmv_dot_kernel(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
-                                const double* __restrict__ v, const double* __restrict__ p, double* __restrict__ y,
-                                double* __restrict__ partial) {
-  __shared__ double sh[32];
-  double acc = 0.0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    double s = 0.0;
-    for (int e = rp[i]; e < rp[i + 1]; e++) s = fma(v[e], p[ci[e]], s);
-    y[i] = s;
-    acc = fma(s, p[i], acc);
-  }
-  double t = block_sum(acc, sh);
-  if (threadIdx.x == 0) partial[blockIdx.x] = t;
-}
-
 __global__ void spmv_kernel(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
                             const double* __restrict__ v, const double* __restrict__ x, double* __restrict__ y) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -573,12 +559,46 @@ __global__ void dot_kernel(int n, const double* __restrict__ a, const double* __
 }
 
 // Sum nparts partials (fixed order) into slot.
+// Sum of partial[0 .. nparts) in the order of one 1024-thread block: virtual thread
+// v adds partial[v], partial[v + 1024], ...; each virtual warp folds its 32 values
+// with an xor butterfly and the 32 warp sums are folded the same way.  Any block
+// whose size divides 1024 gets the same bits (valid in thread 0).
+__device__ double ordered_total(const double* partial, int nparts, double* sh) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int vw = w; vw < 32; vw += nw) {
+    double v = 0.0;
+    for (int q = vw * 32 + lane; q < nparts; q += 1024) v += partial[q];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[vw] = v;
+  }
+  __syncthreads();
+  double t = 0.0;
+  if (w == 0) {
+    t = sh[lane];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  }
+  __syncthreads();
+  return t;
+}
+
 __global__ void finalize_kernel(const double* partial, int nparts, double* slot) {
   __shared__ double sh[32];
-  double s = 0.0;
-  for (int q = threadIdx.x; q < nparts; q += blockDim.x) s += partial[q];
-  double t = block_sum(s, sh);
+  double t = ordered_total(partial, nparts, sh);
   if (threadIdx.x == 0) *slot = t;
+}
+
+// After every block wrote its partial: true in the block that finishes last, which
+// then reads all partials (the fence orders the writes before the ticket).
+__device__ bool last_block_done(unsigned* counter) {
+  __shared__ bool s_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (s_last) __threadfence();
+  return s_last;
 }
 
 // r = b - y; partial ||r||^2
@@ -595,16 +615,12 @@ __global__ void residual_kernel(int n, const double* __restrict__ b, const doubl
   if (threadIdx.x == 0) partial[blockIdx.x] = t;
 }
 
-__global__ void alpha_kernel(double* sc) {
-  double yp = sc[S_YP];
-  if (!(yp > 0.0) || !isfinite(yp)) sc[S_FLAG] = 1.0;
-  sc[S_ALPHA] = sc[S_RZ] / yp;
-}
+
 
 // x += alpha p; r -= alpha y (rold = r first when flexible); partial ||r||^2
-__global__ void update_kernel(int n, const double* __restrict__ sc, const double* __restrict__ p,
+__global__ void update_kernel(int n, double* __restrict__ sc, const double* __restrict__ p,
                               const double* __restrict__ y, double* __restrict__ x, double* __restrict__ r,
-                              double* __restrict__ rold, double* partial) {
+                              double* __restrict__ rold, double* partial, unsigned* counter) {
   __shared__ double sh[32];
   const double alpha = sc[S_ALPHA];
   double acc = 0.0;
@@ -618,11 +634,18 @@ __global__ void update_kernel(int n, const double* __restrict__ sc, const double
   }
   double t = block_sum(acc, sh);
   if (threadIdx.x == 0) partial[blockIdx.x] = t;
+  // r.r total by the last block (same sum as finalize_kernel)
+  if (!last_block_done(counter)) return;
+  const double nr = ordered_total(partial, gridDim.x, sh);
+  if (threadIdx.x == 0) {
+    sc[S_NR] = nr;
+    *counter = 0u;
+  }
 }
 
 // beta (cgcycle.cu:52-54; Polak-Ribiere when flexible); 0 on the first iteration,
 // where p = z.
-__global__ void beta_kernel(double* sc, int flexible) {
+__device__ void beta_update(double* sc, int flexible) {
   double rz = sc[S_RZ], rzn = sc[S_RZNEW];
   if (sc[S_FIRST] != 0.0) {
     sc[S_BETA] = 0.0;
@@ -631,6 +654,76 @@ __global__ void beta_kernel(double* sc, int flexible) {
     sc[S_BETA] = flexible ? (rzn - sc[S_ZROLD]) / rz : rzn / rz;
   }
   sc[S_RZ] = rzn;
+}
+
+__device__ void alpha_update(double* sc) {
+  double yp = sc[S_YP];
+  if (!(yp > 0.0) || !isfinite(yp)) sc[S_FLAG] = 1.0;
+  sc[S_ALPHA] = sc[S_RZ] / yp;
+}
+
+// y = A p and p.y; the last block forms p.y and alpha (same sums as a separate
+// finalize and alpha step).
+__global__ void spmv_dot_kernel(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                const double* __restrict__ v, const double* __restrict__ p, double* __restrict__ y,
+                                double* __restrict__ partial, double* sc, unsigned* counter) {
+  __shared__ double sh[32];
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int e = rp[i]; e < rp[i + 1]; e++) s = fma(v[e], p[ci[e]], s);
+    y[i] = s;
+    acc = fma(s, p[i], acc);
+  }
+  double t = block_sum(acc, sh);
+  if (threadIdx.x == 0) partial[blockIdx.x] = t;
+  if (!last_block_done(counter)) return;
+  const double yp = ordered_total(partial, gridDim.x, sh);
+  if (threadIdx.x == 0) {
+    sc[S_YP] = yp;
+    alpha_update(sc);
+    *counter = 0u;
+  }
+}
+
+// z.r (and z.r_old for the flexible beta) with the totals and beta formed by the
+// last block (same sums as dot_kernel + finalize_kernel + the beta step).
+__global__ void dot_beta_kernel(int n, const double* __restrict__ z, const double* __restrict__ r,
+                                const double* __restrict__ rold, double* partial, double* partial2, double* sc,
+                                int flexible, unsigned* counter) {
+  __shared__ double sh[32];
+  double s1 = 0.0, s2 = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    s1 = fma(z[i], r[i], s1);
+    if (rold) s2 = fma(z[i], rold[i], s2);
+  }
+  double t = block_sum(s1, sh);
+  if (threadIdx.x == 0) partial[blockIdx.x] = t;
+  if (rold) {
+    double t2 = block_sum(s2, sh);
+    if (threadIdx.x == 0) partial2[blockIdx.x] = t2;
+  }
+  if (!last_block_done(counter)) return;
+  const double rzn = ordered_total(partial, gridDim.x, sh);
+  const double zro = rold ? ordered_total(partial2, gridDim.x, sh) : 0.0;
+  if (threadIdx.x == 0) {
+    sc[S_RZNEW] = rzn;
+    if (rold) sc[S_ZROLD] = zro;
+    beta_update(sc, flexible);
+    *counter = 0u;
+  }
+}
+
+// Continue the device-side PCG loop?  Stops on convergence (the host's test:
+// sqrt(r.r) / |b| <= tol), breakdown, a non-finite residual, a smoother copy that
+// timed out, or maxIters.
+__global__ void pcg_check_kernel(double* sc, cudaGraphConditionalHandle loop) {
+  const double it = sc[S_IT] + 1.0;
+  sc[S_IT] = it;
+  const double nr = sqrt(sc[S_NR]);
+  const bool stop = sc[S_FLAG] != 0.0 || sc[S_KERR] != 0.0 || !isfinite(nr) || nr / sc[S_BNORM] <= sc[S_TOL] ||
+                    it >= sc[S_MAXIT];
+  cudaGraphSetConditional(loop, stop ? 0u : 1u);
 }
 
 __global__ void set_slot_kernel(double* sc, int slot, double v) { sc[slot] = v; }
@@ -817,9 +910,10 @@ void stage_mark(Ctx& c, const char* what, int l) {
   c.stage_marks->emplace_back(std::string(what) + " l" + std::to_string(l), e);
 }
 
-// b (level order for l > 0, already permuted for l == 0) -> x (same ordering).
+// b (level order for l > 0, already permuted for l == 0) -> x (same ordering).  At
+// level 0 with z_out != nullptr the result goes to z_out in FP64 instead of x_out.
 template <class T>
-void vcycle(Ctx& c, Hierarchy<T>& H, int l, const T* b_in, T* x_out) {
+void vcycle(Ctx& c, Hierarchy<T>& H, int l, const T* b_in, T* x_out, double* z_out = nullptr) {
   cudaStream_t s = c.stream;
   Level<T>& L = *H.L[l];
   const int n = L.A.n;
@@ -855,6 +949,8 @@ void vcycle(Ctx& c, Hierarchy<T>& H, int l, const T* b_in, T* x_out) {
   stage_mark(c, "post", l);
   if (l > 0) {
     FG_LAUNCH(permute_out_kernel<T>, grid_for(n, 256), 256, 0, s, n, L.iperm.p, L.x.p, x_out);
+  } else if (z_out) {
+    FG_LAUNCH(cast_out_kernel<T>, grid_for(n, 256), 256, 0, s, n, L.x.p, z_out);
   } else {
     FG_CUDA(cudaMemcpyAsync(x_out, L.x.p, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
   }
@@ -871,9 +967,12 @@ void precondition(Ctx& c, Hierarchy<T>& H, const double* r, double* z) {
   T* x = L.coarsest ? L.x.p : L.xo.p;
   FG_LAUNCH(cast_in_kernel<T>, grid_for(n, 256), 256, 0, s, n, r, b);
   stage_mark(c, "cast_in", 0);
-  vcycle(c, H, 0, b, x);
-  FG_LAUNCH(cast_out_kernel<T>, grid_for(n, 256), 256, 0, s, n, x, z);
-  stage_mark(c, "cast_out", 0);
+  if (L.coarsest) {
+    vcycle(c, H, 0, b, x);
+    FG_LAUNCH(cast_out_kernel<T>, grid_for(n, 256), 256, 0, s, n, x, z);
+  } else {
+    vcycle(c, H, 0, b, x, z);  // level 0 writes z itself
+  }
 }
 
 void precondition_any(Ctx& c, const double* r, double* z) {
@@ -895,6 +994,8 @@ void ensure_work(Ctx& c, int n) {
   if (c.red.n == 0) {
     c.red.alloc(2 * kRedBlocks + 64, s);
     c.red.zero();
+    c.rcount.alloc(4, s);
+    c.rcount.zero();
   }
   if (!c.h_scalars) FG_CUDA(cudaMallocHost((void**)&c.h_scalars, 64 * sizeof(double)));
 }
@@ -1069,29 +1170,27 @@ namespace {
 
 // One PCG iteration after the residual check: z = M r, beta, p = z + beta p,
 // y = A p, alpha, x += alpha p, r -= alpha y, ||r||^2, scalars to the host.
-void pcg_iteration_body(Ctx& c, int n, int flexible) {
+void pcg_iteration_body(Ctx& c, int n, int flexible, bool to_host) {
   cudaStream_t s = c.stream;
   double* part = c.red.p;
   double* part2 = c.red.p + kRedBlocks;
   double* sc = c.red.p + 2 * kRedBlocks;
+  unsigned* cnt = c.rcount.p;
   const DCsr<double>& A = c.A0p;
   precondition_any(c, c.vr.p, c.vz.p);
-  FG_LAUNCH(dot_kernel, kRedBlocks, kRedThreads, 0, s, n, c.vz.p, c.vr.p, flexible ? c.vrold.p : nullptr, part,
-            part2);
-  FG_LAUNCH(finalize_kernel, 1, 1024, 0, s, part, kRedBlocks, sc + S_RZNEW);
-  if (flexible) FG_LAUNCH(finalize_kernel, 1, 1024, 0, s, part2, kRedBlocks, sc + S_ZROLD);
-  FG_LAUNCH(beta_kernel, 1, 1, 0, s, sc, flexible);
+  FG_LAUNCH(dot_beta_kernel, kRedBlocks, kRedThreads, 0, s, n, c.vz.p, c.vr.p, flexible ? c.vrold.p : nullptr, part,
+            part2, sc, flexible, cnt);
   FG_LAUNCH(pupdate_kernel, kRedBlocks, kRedThreads, 0, s, n, sc, c.vz.p, c.vp.p);
-  FG_LAUNCH(spmv_dot_kernel, kRedBlocks, kRedThreads, 0, s, n, A.rp.p, A.ci.p, A.v.p, c.vp.p, c.vy.p, part);
-  FG_LAUNCH(finalize_kernel, 1, 1024, 0, s, part, kRedBlocks, sc + S_YP);
-  FG_LAUNCH(alpha_kernel, 1, 1, 0, s, sc);
+  FG_LAUNCH(spmv_dot_kernel, kRedBlocks, kRedThreads, 0, s, n, A.rp.p, A.ci.p, A.v.p, c.vp.p, c.vy.p, part, sc,
+            cnt + 1);
   FG_LAUNCH(update_kernel, kRedBlocks, kRedThreads, 0, s, n, sc, c.vp.p, c.vy.p, c.vx.p, c.vr.p,
-            flexible ? c.vrold.p : nullptr, part);
-  FG_LAUNCH(finalize_kernel, 1, 1024, 0, s, part, kRedBlocks, sc + S_NR);
-  FG_CUDA(cudaMemcpyAsync(c.h_scalars, sc, S_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s));
+            flexible ? c.vrold.p : nullptr, part, cnt + 2);
+  if (to_host) FG_CUDA(cudaMemcpyAsync(c.h_scalars, sc, S_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s));
 }
 
-// Captures the iteration body once per hierarchy as a CUDA graph.
+// Captures the whole PCG loop once per hierarchy as a CUDA graph: a conditional while
+// node whose body is one iteration followed by pcg_check_kernel, so the iterations
+// run back to back on the device with no host round trip.
 bool capture_iteration(Ctx& c, int n, int flexible) {
   if (c.pcg_exec && c.graph_gen == c.hier_gen && c.graph_flexible == flexible) return true;
   if (c.pcg_exec) {
@@ -1100,35 +1199,45 @@ bool capture_iteration(Ctx& c, int n, int flexible) {
   }
   cudaStream_t s = c.stream;
   int64_t before = g_kernel_launches.load();
-  if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
-    (void)cudaGetLastError();
-    return false;
-  }
   cudaGraph_t g = nullptr;
-  try {
-    pcg_iteration_body(c, n, flexible);
-  } catch (...) {
-    cudaStreamEndCapture(s, &g);
+  auto fail = [&]() {
+    (void)cudaGetLastError();
     if (g) cudaGraphDestroy(g);
-    (void)cudaGetLastError();
     g_kernel_launches.store(before);
     return false;
+  };
+  if (cudaGraphCreate(&g, 0) != cudaSuccess) return fail();
+  cudaGraphConditionalHandle loop;
+  if (cudaGraphConditionalHandleCreate(&loop, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) return fail();
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = loop;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  if (cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp) != cudaSuccess) return fail();
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  if (cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+    return fail();
+  try {
+    pcg_iteration_body(c, n, flexible, false);
+    FG_LAUNCH(pcg_check_kernel, 1, 1, 0, s, c.red.p + 2 * kRedBlocks, loop);
+  } catch (...) {
+    cudaGraph_t dummy = nullptr;
+    cudaStreamEndCapture(s, &dummy);
+    return fail();
   }
-  if (cudaStreamEndCapture(s, &g) != cudaSuccess || !g) {
-    (void)cudaGetLastError();
-    g_kernel_launches.store(before);
-    return false;
-  }
+  cudaGraph_t captured = nullptr;
+  if (cudaStreamEndCapture(s, &captured) != cudaSuccess) return fail();
   cudaError_t e = cudaGraphInstantiate(&c.pcg_exec, g, 0);
   cudaGraphDestroy(g);
+  g = nullptr;
   if (e != cudaSuccess) {
-    (void)cudaGetLastError();
     c.pcg_exec = nullptr;
-    g_kernel_launches.store(before);
-    return false;
+    return fail();
   }
-  c.graph_nodes = g_kernel_launches.load() - before;
-  g_kernel_launches.store(before);  // counted per replay below
+  c.graph_nodes = g_kernel_launches.load() - before;  // kernels of one iteration
+  g_kernel_launches.store(before);  // counted per iteration after each solve
   c.graph_gen = c.hier_gen;
   c.graph_flexible = flexible;
   return true;
@@ -1185,25 +1294,37 @@ SolveResult amg_solve_device(Ctx& c, const double* d_b, double* d_x) {
   if (nr / bnorm <= tol) {
     res.status = FEMGPU_OK;
   } else {
-    const bool graph = capture_iteration(c, n, flexible);
-    while (it < c.cfg.maxIters) {
-      if (graph) {
-        FG_CUDA(cudaGraphLaunch(c.pcg_exec, s));
-        g_kernel_launches.fetch_add(c.graph_nodes);
-      } else {
-        pcg_iteration_body(c, n, flexible);
-      }
+    const bool graph = c.cfg.maxIters > 0 && capture_iteration(c, n, flexible);
+    if (graph) {
+      // the device runs the iterations until pcg_check_kernel stops the loop
+      FG_LAUNCH(set_slot_kernel, 1, 1, 0, s, sc, S_IT, 0.0);
+      FG_LAUNCH(set_slot_kernel, 1, 1, 0, s, sc, S_BNORM, bnorm);
+      FG_LAUNCH(set_slot_kernel, 1, 1, 0, s, sc, S_TOL, tol);
+      FG_LAUNCH(set_slot_kernel, 1, 1, 0, s, sc, S_MAXIT, (double)c.cfg.maxIters);
+      FG_CUDA(cudaGraphLaunch(c.pcg_exec, s));
+      FG_CUDA(cudaMemcpyAsync(c.h_scalars, sc, S_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s));
       FG_CUDA(cudaStreamSynchronize(s));
-      it++;
+      it = (int)c.h_scalars[S_IT];
+      g_kernel_launches.fetch_add(c.graph_nodes * it);
       nr = sqrt(c.h_scalars[S_NR]);
       FG_REQUIRE(c.h_scalars[S_KERR] == 0.0, FEMGPU_ERR_LIMIT, "smoother copy wait ran out");
-      if (c.h_scalars[S_FLAG] != 0.0 || !std::isfinite(nr)) {
-        res.status = FEMGPU_ERR_BREAKDOWN;
-        break;
-      }
-      if (nr / bnorm <= tol) {
-        res.status = FEMGPU_OK;
-        break;
+      if (c.h_scalars[S_FLAG] != 0.0 || !std::isfinite(nr)) res.status = FEMGPU_ERR_BREAKDOWN;
+      else if (nr / bnorm <= tol) res.status = FEMGPU_OK;
+    } else {
+      while (it < c.cfg.maxIters) {
+        pcg_iteration_body(c, n, flexible, true);
+        FG_CUDA(cudaStreamSynchronize(s));
+        it++;
+        nr = sqrt(c.h_scalars[S_NR]);
+        FG_REQUIRE(c.h_scalars[S_KERR] == 0.0, FEMGPU_ERR_LIMIT, "smoother copy wait ran out");
+        if (c.h_scalars[S_FLAG] != 0.0 || !std::isfinite(nr)) {
+          res.status = FEMGPU_ERR_BREAKDOWN;
+          break;
+        }
+        if (nr / bnorm <= tol) {
+          res.status = FEMGPU_OK;
+          break;
+        }
       }
     }
   }
@@ -1286,7 +1407,7 @@ void profile_kernel(Ctx& c, int which, int reps, double* ms, double* bytes) {
     FG_LAUNCH(fill_value_kernel<double>, grid_for(n, 256), 256, 0, s, (int64_t)n, c.vp.p, 1.0);
     auto run = [&]() {
       FG_LAUNCH(spmv_dot_kernel, kRedBlocks, kRedThreads, 0, s, n, c.A0p.rp.p, c.A0p.ci.p, c.A0p.v.p, c.vp.p, c.vy.p,
-                c.red.p);
+                c.red.p, c.red.p + 2 * kRedBlocks, c.rcount.p + 1);
     };
     for (int i = 0; i < 3; i++) run();
     cudaEvent_t e0, e1;

@@ -129,6 +129,7 @@ struct Ctx {
   // PCG work vectors (permuted order)
   DBuf<double> vb, vx, vr, vz, vp, vy, vrold;
   DBuf<double> red;              // reduction partials + scalars
+  DBuf<unsigned> rcount;         // last-block tickets of the fused reductions
   double* h_scalars = nullptr;   // pinned host mirror of the device scalars
   // one PCG iteration captured as a CUDA graph, rebuilt when the hierarchy changes
   uint64_t hier_gen = 0, graph_gen = ~0ull;
