@@ -384,20 +384,26 @@ __global__ void node_degree_to_agg_kernel(int n, const int32_t* xadj, const int3
   if (i < n) atomicAdd(&cnt[fine[i]], xadj[i + 1] - xadj[i]);
 }
 
-__global__ void induced_candidates_kernel(int nagg, const int32_t* astart, const int32_t* members,
-                                          const int32_t* xadj, const int32_t* adj, const int32_t* fine,
-                                          const int32_t* coff, int32_t* cand) {
-  int a = blockIdx.x * blockDim.x + threadIdx.x;
-  if (a >= nagg) return;
-  int o = coff[a], end = coff[a + 1];
-  for (int q = astart[a]; q < astart[a + 1]; q++) {
-    int i = members[q];
-    for (int e = xadj[i]; e < xadj[i + 1]; e++) {
-      int b = fine[adj[e]];
-      if (b != a) cand[o++] = b;
-    }
+// Degree of each member node, in member order (aggregates in order, members ascending).
+__global__ void member_degree_kernel(int n, const int32_t* members, const int32_t* xadj, int32_t* deg) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) deg[q] = xadj[members[q] + 1] - xadj[members[q]];
+}
+
+// One thread per member node: the aggregates of its neighbours go to the node's slice
+// of its aggregate's candidate list (its own aggregate as INT32_MAX padding), so every
+// list holds the same multiset as a member-by-member walk.
+__global__ void induced_candidates_nodes_kernel(int n, const int32_t* members, const int32_t* noff,
+                                                const int32_t* __restrict__ xadj, const int32_t* __restrict__ adj,
+                                                const int32_t* __restrict__ fine, int32_t* cand) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int i = members[q], a = fine[i];
+  int o = noff[q];
+  for (int e = xadj[i]; e < xadj[i + 1]; e++) {
+    const int b = fine[adj[e]];
+    cand[o++] = b != a ? b : INT32_MAX;
   }
-  while (o < end) cand[o++] = INT32_MAX;  // padding, removed after the unique sort
 }
 
 __global__ void drop_padding_kernel(int nseg, const int32_t* off, int32_t* cnt, const int32_t* vals) {
@@ -509,8 +515,13 @@ void old_mis(Ctx& c, int n, const int32_t* xadj, const int32_t* adj, OldMisOut& 
   FG_LAUNCH(node_degree_to_agg_kernel, grid_for(n, 256), 256, 0, s, n, xadj, fine.p, ccount.p);
   int64_t ncand = exclusive_scan(ccount.p, coff.p, nagg, s);
   DBuf<int32_t> cand(ncand > 0 ? ncand : 1, s), ucount(nagg + 1, s), ixadj(nagg + 1, s);
-  FG_LAUNCH(induced_candidates_kernel, grid_for(nagg, 128), 128, 0, s, nagg, astart.p, members.p, xadj, adj, fine.p,
-            coff.p, cand.p);
+  {
+    DBuf<int32_t> mdeg(n + 1, s), noff(n + 1, s);
+    FG_LAUNCH(member_degree_kernel, grid_for(n, 256), 256, 0, s, n, members.p, xadj, mdeg.p);
+    exclusive_scan(mdeg.p, noff.p, n, s);
+    FG_LAUNCH(induced_candidates_nodes_kernel, grid_for(n, 256), 256, 0, s, n, members.p, noff.p, xadj, adj, fine.p,
+              cand.p);
+  }
   segmented_sort_i32(cand.p, coff.p, nagg, ucount.p, s);
   FG_LAUNCH(drop_padding_kernel, grid_for(nagg, 256), 256, 0, s, nagg, coff.p, ucount.p, cand.p);
   int64_t innz = exclusive_scan(ucount.p, ixadj.p, nagg, s);

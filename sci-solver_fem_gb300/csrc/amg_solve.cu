@@ -662,18 +662,36 @@ __device__ void alpha_update(double* sc) {
   sc[S_ALPHA] = sc[S_RZ] / yp;
 }
 
-// y = A p and p.y; the last block forms p.y and alpha (same sums as a separate
-// finalize and alpha step).
+// The outer PCG's y = A p and p.y, one thread per row over a fixed grid; the last
+// block forms p.y and alpha (same sums as a separate finalize and alpha step).
 __global__ void spmv_dot_kernel(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
-                                const double* __restrict__ v, const double* __restrict__ p, double* __restrict__ y,
-                                double* __restrict__ partial, double* sc, unsigned* counter) {
+                                      const double* __restrict__ v, const double* __restrict__ p,
+                                      double* __restrict__ y, double* __restrict__ partial, double* sc,
+                                      unsigned* counter) {
   __shared__ double sh[32];
   double acc = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int a = rp[i], b = rp[i + 1];
+    const double pi = p[i];
     double s = 0.0;
-    for (int e = rp[i]; e < rp[i + 1]; e++) s = fma(v[e], p[ci[e]], s);
+    // entries in groups of 8: all columns and values, then all gathers, then the
+    // fused multiply-adds in entry order
+    for (int e0 = a; e0 < b; e0 += 8) {
+      int c[8];
+      double w[8], x[8];
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        c[k] = e0 + k < b ? ci[e0 + k] : 0;
+        w[k] = e0 + k < b ? v[e0 + k] : 0.0;
+      }
+#pragma unroll
+      for (int k = 0; k < 8; k++) x[k] = e0 + k < b ? p[c[k]] : 0.0;
+#pragma unroll
+      for (int k = 0; k < 8; k++)
+        if (e0 + k < b) s = fma(w[k], x[k], s);
+    }
     y[i] = s;
-    acc = fma(s, p[i], acc);
+    acc = fma(s, pi, acc);
   }
   double t = block_sum(acc, sh);
   if (threadIdx.x == 0) partial[blockIdx.x] = t;
@@ -1170,6 +1188,13 @@ namespace {
 
 // One PCG iteration after the residual check: z = M r, beta, p = z + beta p,
 // y = A p, alpha, x += alpha p, r -= alpha y, ||r||^2, scalars to the host.
+// y = A0p p with p.y and alpha.
+void launch_spmv_dot(Ctx& c, int n, const double* p, double* y) {
+  const DCsr<double>& A = c.A0p;
+  FG_LAUNCH(spmv_dot_kernel, kRedBlocks, kRedThreads, 0, c.stream, n, A.rp.p, A.ci.p, A.v.p, p, y, c.red.p,
+            c.red.p + 2 * kRedBlocks, c.rcount.p + 1);
+}
+
 void pcg_iteration_body(Ctx& c, int n, int flexible, bool to_host) {
   cudaStream_t s = c.stream;
   double* part = c.red.p;
@@ -1181,8 +1206,7 @@ void pcg_iteration_body(Ctx& c, int n, int flexible, bool to_host) {
   FG_LAUNCH(dot_beta_kernel, kRedBlocks, kRedThreads, 0, s, n, c.vz.p, c.vr.p, flexible ? c.vrold.p : nullptr, part,
             part2, sc, flexible, cnt);
   FG_LAUNCH(pupdate_kernel, kRedBlocks, kRedThreads, 0, s, n, sc, c.vz.p, c.vp.p);
-  FG_LAUNCH(spmv_dot_kernel, kRedBlocks, kRedThreads, 0, s, n, A.rp.p, A.ci.p, A.v.p, c.vp.p, c.vy.p, part, sc,
-            cnt + 1);
+  launch_spmv_dot(c, n, c.vp.p, c.vy.p);
   FG_LAUNCH(update_kernel, kRedBlocks, kRedThreads, 0, s, n, sc, c.vp.p, c.vy.p, c.vx.p, c.vr.p,
             flexible ? c.vrold.p : nullptr, part, cnt + 2);
   if (to_host) FG_CUDA(cudaMemcpyAsync(c.h_scalars, sc, S_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -1404,10 +1428,9 @@ void profile_kernel(Ctx& c, int which, int reps, double* ms, double* bytes) {
   if (which == 0) {
     const int n = c.A.n;
     ensure_work(c, n);
-    FG_LAUNCH(fill_value_kernel<double>, grid_for(n, 256), 256, 0, s, (int64_t)n, c.vp.p, 1.0);
+      FG_LAUNCH(fill_value_kernel<double>, grid_for(n, 256), 256, 0, s, (int64_t)n, c.vp.p, 1.0);
     auto run = [&]() {
-      FG_LAUNCH(spmv_dot_kernel, kRedBlocks, kRedThreads, 0, s, n, c.A0p.rp.p, c.A0p.ci.p, c.A0p.v.p, c.vp.p, c.vy.p,
-                c.red.p, c.red.p + 2 * kRedBlocks, c.rcount.p + 1);
+      launch_spmv_dot(c, n, c.vp.p, c.vy.p);
     };
     for (int i = 0; i < 3; i++) run();
     cudaEvent_t e0, e1;
