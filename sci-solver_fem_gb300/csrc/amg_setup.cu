@@ -27,6 +27,36 @@ namespace {
 
 constexpr int kCap = 100000;  // bound on every data-dependent loop (error, never spin)
 
+// Setup phase timer (FEMGPU_PROFILE): stream-synchronised wall time per phase with
+// the kernel launches and host reads it took.
+struct PhaseTimer {
+  bool on;
+  cudaStream_t s;
+  int level;
+  std::chrono::steady_clock::time_point t0;
+  int64_t syncs0 = 0, launches0 = 0;
+  PhaseTimer(cudaStream_t st, int lvl) : on(getenv("FEMGPU_PROFILE") != nullptr), s(st), level(lvl) {
+    if (on) {
+      cudaStreamSynchronize(s);
+      t0 = std::chrono::steady_clock::now();
+      syncs0 = g_host_syncs.load();
+      launches0 = g_kernel_launches.load();
+    }
+  }
+  void mark(const char* what) {
+    if (!on) return;
+    cudaStreamSynchronize(s);
+    auto t = std::chrono::steady_clock::now();
+    const int64_t sy = g_host_syncs.load(), la = g_kernel_launches.load();
+    fprintf(stderr, "[femgpu setup] level %d %-10s %8.3f ms  %5lld launches %4lld host reads\n", level, what,
+            std::chrono::duration<double, std::milli>(t - t0).count(), (long long)(la - launches0),
+            (long long)(sy - syncs0));
+    t0 = t;
+    syncs0 = sy;
+    launches0 = la;
+  }
+};
+
 // ---------------------------------------------------------------------------------
 // glibc rand() stream (TYPE_3 additive feedback generator), host side: the
 // reference draws 32768 seeds with rand() after srand() (randomizedMIS_GPU.cu:195-201).
@@ -65,81 +95,89 @@ __global__ void mis_randoms_kernel(int n, int iterations, uint32_t* randoms, con
     }
 }
 
-__global__ void mis_first_init_kernel(int n, const uint32_t* randoms, int32_t* best, int32_t* origin) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) {
-    origin[i] = i;
-    best[i] = (int32_t)(randoms[i] % 1000000u);
-  }
+// A node's (value, origin) pair packed as value << 32 | origin: the reference's update
+// (take a neighbour with a larger value, or the same positive value and a larger
+// origin) is the maximum of the packed keys over the node and its neighbours with a
+// positive value.
+__device__ __forceinline__ uint64_t mis_key(int32_t best, int32_t origin) {
+  return ((uint64_t)(uint32_t)best << 32) | (uint32_t)origin;
 }
 
-__global__ void mis_init_kernel(int n, uint32_t* randoms, int32_t* best, int32_t* origin, const int32_t* mis) {
+__global__ void mis_first_init_kernel(int n, const uint32_t* randoms, uint64_t* key) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) key[i] = mis_key((int32_t)(randoms[i] % 1000000u), i);
+}
+
+__global__ void mis_init_kernel(int n, uint32_t* randoms, uint64_t* key, const int32_t* mis) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) {
     uint32_t z = taus(randoms[i]);
-    origin[i] = i;
     int st = mis[i];
-    best[i] = st == -1 ? (int32_t)(z % 1000000u) : (st == 1 ? 1000001 : 0);
+    key[i] = mis_key(st == -1 ? (int32_t)(z % 1000000u) : (st == 1 ? 1000001 : 0), i);
     randoms[i] = z;
   }
 }
 
-__global__ void mis_iterate_kernel(int n, const int32_t* __restrict__ oin, int32_t* __restrict__ oout,
-                                   const int32_t* __restrict__ bin, int32_t* __restrict__ bout,
+__global__ void mis_iterate_kernel(int n, const uint64_t* __restrict__ kin, uint64_t* __restrict__ kout,
                                    const int32_t* __restrict__ xadj, const int32_t* __restrict__ adj, int32_t* mis,
                                    int32_t* incomplete, int final_pass) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  int best = bin[i], org = oin[i];
-  if (best < 1000001) {
-    for (int e = xadj[i]; e < xadj[i + 1]; e++) {
-      int nb = adj[e];
-      int ch = bin[nb], cho = oin[nb];
-      if (ch > 0 && ch == best && cho > org) org = cho;
-      if (ch > best) {
-        best = ch;
-        org = cho;
-      }
+  uint64_t k = kin[i];
+  if ((k >> 32) < 1000001u) {
+    // neighbours in groups of 8: all indices, then all keys, so the loads overlap
+    const int e1 = xadj[i + 1];
+    for (int e0 = xadj[i]; e0 < e1; e0 += 8) {
+      int nb[8];
+      uint64_t kn[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) nb[q] = e0 + q < e1 ? adj[e0 + q] : i;
+#pragma unroll
+      for (int q = 0; q < 8; q++) kn[q] = kin[nb[q]];
+#pragma unroll
+      for (int q = 0; q < 8; q++)
+        if ((kn[q] >> 32) > 0u && kn[q] > k) k = kn[q];
     }
   }
-  bout[i] = best;
-  oout[i] = org;
+  kout[i] = k;
   if (final_pass) {
+    const int best = (int)(k >> 32), org = (int)(uint32_t)k;
     int st = -1;
     if (org == i) st = 1;
     else if (best == 1000001) st = 0;
     mis[i] = st;
-    if (st == -1) *incomplete = 1;
+    // one store per warp with an undecided node (a single flag address)
+    const unsigned undecided = __ballot_sync(__activemask(), st == -1);
+    if (undecided && (threadIdx.x & 31) == (__ffs(__activemask()) - 1)) *incomplete = 1;
   }
 }
 
 void random_mis(Ctx& c, int n, const int32_t* xadj, const int32_t* adj, int k, DBuf<int32_t>& mis) {
   cudaStream_t s = c.stream;
+  PhaseTimer pt(s, -5);
   mis.alloc(n, s);
   fill_i32(mis.p, n, -1, s);
   std::vector<uint32_t> seeds;
   glibc_rand_stream(c.cfg.seed, 32768, seeds);
   DBuf<uint32_t> dseeds(32768, s), randoms(n, s);
   dseeds.upload(seeds.data(), 32768);
-  DBuf<int32_t> b0(n, s), b1(n, s), o0(n, s), o1(n, s), flag(1, s);
+  DBuf<uint64_t> k0(n, s), k1(n, s);
+  DBuf<int32_t> flag(1, s);
   FG_LAUNCH(mis_randoms_kernel, 128, 256, 0, s, n, (n + 32767) / 32768, randoms.p, dseeds.p);
-  FG_LAUNCH(mis_first_init_kernel, grid_for(n, 256), 256, 0, s, n, randoms.p, b0.p, o0.p);
+  FG_LAUNCH(mis_first_init_kernel, grid_for(n, 256), 256, 0, s, n, randoms.p, k0.p);
+  pt.mark("mis init");
   for (int round = 0;; round++) {
     FG_REQUIRE(round < kCap, FEMGPU_ERR_LIMIT, "randomized MIS did not complete");
-    if (round > 0) FG_LAUNCH(mis_init_kernel, grid_for(n, 256), 256, 0, s, n, randoms.p, b0.p, o0.p, mis.p);
+    if (round > 0) FG_LAUNCH(mis_init_kernel, grid_for(n, 256), 256, 0, s, n, randoms.p, k0.p, mis.p);
     flag.zero();
-    int32_t *bi = b0.p, *bo = b1.p, *oi = o0.p, *oo = o1.p;
+    uint64_t *ki = k0.p, *ko = k1.p;
     for (int it = 0; it < k; it++) {
-      FG_LAUNCH(mis_iterate_kernel, grid_for(n, 256), 256, 0, s, n, oi, oo, bi, bo, xadj, adj, mis.p, flag.p,
-                it == k - 1);
-      std::swap(bi, bo);
-      std::swap(oi, oo);
+      FG_LAUNCH(mis_iterate_kernel, grid_for(n, 256), 256, 0, s, n, ki, ko, xadj, adj, mis.p, flag.p, it == k - 1);
+      std::swap(ki, ko);
     }
-    if (bi != b0.p) {  // keep b0/o0 as the next round's input buffers
-      std::swap(b0.p, b1.p);
-      std::swap(o0.p, o1.p);
-    }
+    if (ki != k0.p) std::swap(k0.p, k1.p);  // keep k0 as the next round's input
     if (read_scalar(flag.p, s) == 0) break;
+    pt.mark("mis round");
   }
 }
 
@@ -159,27 +197,41 @@ __global__ void label_roots_kernel(int n, const int32_t* mis, const int32_t* inc
 __global__ void allocate_kernel(int n, const int32_t* __restrict__ xadj, const int32_t* __restrict__ adj,
                                 const int32_t* __restrict__ pin, int32_t* __restrict__ pout, int32_t* aggregated,
                                 int32_t* counters /* [0] unallocated after, [1] changed */) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  int p = pin[i];
-  if (aggregated[i] == 0) {
-    int add = -1;
-    for (int e = xadj[i]; e < xadj[i + 1]; e++) {
-      int cnd = pin[adj[e]];
-      if (cnd != -1) {
-        add = cnd;
-        break;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool changed = false, left = false;
+  if (i < n) {
+    int p = pin[i];
+    if (aggregated[i] == 0) {
+      int add = -1;
+      // first aggregated neighbour in adjacency order, neighbours loaded 8 at a time
+      const int e1 = xadj[i + 1];
+      for (int e0 = xadj[i]; e0 < e1 && add == -1; e0 += 8) {
+        int nb[8], cnd[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) nb[q] = e0 + q < e1 ? adj[e0 + q] : -1;
+#pragma unroll
+        for (int q = 0; q < 8; q++) cnd[q] = nb[q] >= 0 ? pin[nb[q]] : -1;
+#pragma unroll
+        for (int q = 0; q < 8; q++)
+          if (add == -1 && cnd[q] != -1) add = cnd[q];
+      }
+      p = add;
+      if (add != -1) {
+        aggregated[i] = 1;
+        changed = true;
+      } else {
+        left = true;
       }
     }
-    p = add;
-    if (add != -1) {
-      aggregated[i] = 1;
-      atomicExch(&counters[1], 1);
-    } else {
-      atomicAdd(&counters[0], 1);
-    }
+    pout[i] = p;
   }
-  pout[i] = p;
+  // one atomic per block instead of one per node (a single counter address)
+  const int nleft = __syncthreads_count(left);
+  const int nchanged = __syncthreads_or(changed);
+  if (threadIdx.x == 0) {
+    if (nleft) atomicAdd(&counters[0], nleft);
+    if (nchanged) atomicExch(&counters[1], 1);
+  }
 }
 
 __global__ void histogram_kernel(int n, const int32_t* part, const int32_t* w, int32_t* sizes) {
@@ -334,8 +386,10 @@ int restrict_partitions(Ctx& c, int max_size, int full_size, int n, const int32_
 void aggregate(Ctx& c, int n, const int32_t* xadj, const int32_t* adj, int depth, bool weighted, int min_size,
                int max_size, int full_size, const int32_t* weights, DBuf<int32_t>& part) {
   cudaStream_t s = c.stream;
+  PhaseTimer pt(s, -4);
   DBuf<int32_t> mis;
   random_mis(c, n, xadj, adj, depth, mis);
+  pt.mark("mis");
   DBuf<int32_t> incl(n + 1, s), aggregated(n, s), pout(n, s), counters(2, s);
   FG_CUDA(cudaMemcpyAsync(incl.p, mis.p, n * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
   inclusive_scan_inplace(incl.p, n, s);
@@ -352,6 +406,7 @@ void aggregate(Ctx& c, int n, const int32_t* xadj, const int32_t* adj, int depth
     counters.download(h, 2);
     FG_CUDA(cudaStreamSynchronize(s));
     g_host_syncs.fetch_add(1, std::memory_order_relaxed);
+    pt.mark("allocate");
     if (h[0] == 0) {
       if (!weighted) {
         if (remove_small_parts(c, n, part, nullptr, 0, min_size, full_size, aggregated) == 0) return;
@@ -457,33 +512,6 @@ __global__ void node_order_kernel(int nagg, const int32_t* old_of, const int32_t
 
 // Opt-in setup phase timing (environment FEMGPU_PROFILE set): synchronizes between
 // phases and prints the host wall time of each to stderr.
-struct PhaseTimer {
-  bool on;
-  cudaStream_t s;
-  int level;
-  std::chrono::steady_clock::time_point t0;
-  int64_t syncs0 = 0, launches0 = 0;
-  PhaseTimer(cudaStream_t st, int lvl) : on(getenv("FEMGPU_PROFILE") != nullptr), s(st), level(lvl) {
-    if (on) {
-      cudaStreamSynchronize(s);
-      t0 = std::chrono::steady_clock::now();
-      syncs0 = g_host_syncs.load();
-      launches0 = g_kernel_launches.load();
-    }
-  }
-  void mark(const char* what) {
-    if (!on) return;
-    cudaStreamSynchronize(s);
-    auto t = std::chrono::steady_clock::now();
-    const int64_t sy = g_host_syncs.load(), la = g_kernel_launches.load();
-    fprintf(stderr, "[femgpu setup] level %d %-10s %8.3f ms  %5lld launches %4lld host reads\n", level, what,
-            std::chrono::duration<double, std::milli>(t - t0).count(), (long long)(la - launches0),
-            (long long)(sy - syncs0));
-    t0 = t;
-    syncs0 = sy;
-    launches0 = la;
-  }
-};
 
 struct OldMisOut {
   int nagg = 0, npart = 0;
@@ -1016,17 +1044,17 @@ void run_esc_sort(Ctx& c, EscArgs<T> a, int nrows_out, int ncols_out, DCsr<T>& o
     gmark.alloc((size_t)dgrid * ncols_out, s);
   }
   if (ad.nbig > 0 && dense_shared && dsm > 48 * 1024) {
-    FG_CUDA(cudaFuncSetAttribute(esc_dense_kernel<T, MODE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm));
-    FG_CUDA(cudaFuncSetAttribute(esc_dense_kernel<T, MODE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm));
+    ensure_smem(esc_dense_kernel<T, MODE, false>, dsm);
+    ensure_smem(esc_dense_kernel<T, MODE, true>, dsm);
   }
   const size_t wsm = (size_t)kEscWarps * kEscWarpCap * (sizeof(unsigned long long) + sizeof(T));
   const size_t bsm = (size_t)kEscBlockCap * (sizeof(unsigned long long) + sizeof(T));
   static bool attr_set = false;
   if (!attr_set) {
-    FG_CUDA(cudaFuncSetAttribute(esc_warp_kernel<T, MODE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
-    FG_CUDA(cudaFuncSetAttribute(esc_warp_kernel<T, MODE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
-    FG_CUDA(cudaFuncSetAttribute(esc_block_kernel<T, MODE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsm));
-    FG_CUDA(cudaFuncSetAttribute(esc_block_kernel<T, MODE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsm));
+    ensure_smem(esc_warp_kernel<T, MODE, false>, wsm);
+    ensure_smem(esc_warp_kernel<T, MODE, true>, wsm);
+    ensure_smem(esc_block_kernel<T, MODE, false>, bsm);
+    ensure_smem(esc_block_kernel<T, MODE, true>, bsm);
     attr_set = true;
   }
   const int wgrid = std::min<int64_t>((nrows_out + kEscWarps - 1) / kEscWarps, 152 * 64);
@@ -1434,7 +1462,7 @@ void run_spgemm_hash(Ctx& c, EscArgs<T> a, int nrows_out, int ncols_out, DCsr<T>
   const int n1 = read_scalar(nover1.p, s);
   if (n1 > 0) {
     const size_t bsm = (size_t)kHashBlockCap * (sizeof(unsigned long long) + sizeof(T) + sizeof(int32_t));
-    FG_CUDA(cudaFuncSetAttribute(hash_block_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsm));
+    ensure_smem(hash_block_kernel<T>, bsm);
     FG_LAUNCH(hash_block_kernel<T>, std::min(n1, 152 * 2), kHashBlockThreads, bsm, s, a, over1.p, n1, toff.p, tci.p,
               tv.p, cnt.p, over2.p, nover2.p);
     const int n2 = read_scalar(nover2.p, s);
@@ -1446,8 +1474,8 @@ void run_spgemm_hash(Ctx& c, EscArgs<T> a, int nrows_out, int ncols_out, DCsr<T>
       ad.nbig = n2;
       ad.big_rows = over2.p;
       if (dsm > 48 * 1024) {
-        FG_CUDA(cudaFuncSetAttribute(esc_dense_kernel<T, ESC_SPGEMM, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm));
-        FG_CUDA(cudaFuncSetAttribute(esc_dense_kernel<T, ESC_SPGEMM, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm));
+        ensure_smem(esc_dense_kernel<T, ESC_SPGEMM, false>, dsm);
+        ensure_smem(esc_dense_kernel<T, ESC_SPGEMM, true>, dsm);
       }
       ad.counts = cnt.p;
       FG_LAUNCH((esc_dense_kernel<T, ESC_SPGEMM, false>), std::min(n2, 304), 256, dsm, s, ad, ncols_out, nullptr,
@@ -1816,7 +1844,7 @@ void build_levels(Ctx& c, Hierarchy<T>& H) {
       const size_t fbytes = (size_t)N * N * sizeof(double);
       if (fbytes <= 200 * 1024) {
         if (fbytes > 48 * 1024)
-          FG_CUDA(cudaFuncSetAttribute(dense_lu_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fbytes));
+          ensure_smem(dense_lu_smem_kernel, fbytes);
         FG_LAUNCH(dense_lu_smem_kernel, 1, 1024, fbytes, s, N, F.p, piv.p, st.p);
       } else {
         FG_LAUNCH(dense_lu_kernel, 1, 1024, 0, s, N, F.p, piv.p, st.p);
@@ -1825,7 +1853,7 @@ void build_levels(Ctx& c, Hierarchy<T>& H) {
       L.Ainv.alloc((size_t)N * N, s);
       const size_t bbytes = (size_t)N * sizeof(double);
       if (bbytes > 48 * 1024)
-        FG_CUDA(cudaFuncSetAttribute(dense_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bbytes));
+        ensure_smem(dense_inverse_kernel, bbytes);
       FG_LAUNCH(dense_inverse_kernel, N, std::min(1024, std::max(32, (N + 31) / 32 * 32)), bbytes, s, N, F.p, piv.p,
                 L.Ainv.p);
       L.b.alloc(N, s);
@@ -1886,6 +1914,7 @@ void build_levels(Ctx& c, Hierarchy<T>& H) {
       DBuf<int32_t> rlen(N + 1, s);
       FG_LAUNCH(row_lengths_kernel, grid_for(N, 256), 256, 0, s, N, L.Ain.rp.p, rlen.p);
       L.max_in_row = reduce_max(rlen.p, N, s);
+      pt.mark("split rows");
       if (smoother_in_registers(L.max_in_row, L.max_part_rows)) {
         build_smoother_groups(c, L, kRegGroupRows, std::numeric_limits<int>::max());
         L.ci16.alloc(L.Ain.nnz + 16, s);
@@ -1894,7 +1923,9 @@ void build_levels(Ctx& c, Hierarchy<T>& H) {
           FG_LAUNCH(group_local_cols_kernel, L.ngroups, 256, 0, s, L.grows.p, L.Ain.rp.p, L.Ain.ci.p, L.ci16.p);
       } else
         build_smoother_groups(c, L, L.max_part_rows, L.max_part_entries);
+      pt.mark("groups");
       plan_smoother(c, L);
+      pt.mark("plan");
       if (pt.on)
         fprintf(stderr,
                 "[femgpu setup] level %d smoother: %s, groups %d (max %d rows), lanes %d, cluster %d, "

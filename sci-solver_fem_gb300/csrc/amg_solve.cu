@@ -887,7 +887,7 @@ void smooth_sweeps(Ctx& c, Level<T>& L, bool post, const T* b, const T* xin, T* 
   if (smoother_in_registers(L.max_in_row, L.max_part_rows)) {
     auto k = post ? smooth_reg_kernel<T, true, kRegRow> : smooth_reg_kernel<T, false, kRegRow>;
     if (L.smooth_smem > 48 * 1024)
-      FG_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smooth_smem));
+      ensure_smem(k, L.smooth_smem);
     FG_LAUNCH(k, L.smooth_grid, L.smooth_threads, L.smooth_smem, s, L.ngroups, L.grows.p, L.Ain.rp.p, L.ci16.p,
               L.Ain.v.p, L.diag.p, L.dinv.p, b, w, inner, xin, xout, rout, L.max_group_ents + 16,
               c.red.p + 2 * kRedBlocks + S_KERR);
@@ -896,7 +896,7 @@ void smooth_sweeps(Ctx& c, Level<T>& L, bool post, const T* b, const T* xin, T* 
   if (L.smooth_k > 0) {
     CregSmoothFn<T> k = pick_creg_kernel<T>(post, L.smooth_lanes, L.smooth_k);
     if (L.smooth_smem > 48 * 1024)
-      FG_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smooth_smem));
+      ensure_smem(k, L.smooth_smem);
     launch_clustered(k, L.ngroups * L.cluster, L.smooth_threads, L.smooth_smem, L.cluster, s,
                      (const int32_t*)L.grows.p, (const int32_t*)L.Ain.rp.p, (const int32_t*)L.Ain.ci.p,
                      (const T*)L.Ain.v.p, (const T*)L.diag.p, (const T*)L.dinv.p, b, w, inner, xin, xout, rout,
@@ -906,7 +906,7 @@ void smooth_sweeps(Ctx& c, Level<T>& L, bool post, const T* b, const T* xin, T* 
   ClusterSmoothFn<T> k = pick_cluster_kernel<T>(post, L.smooth_staged, L.smooth_lanes);
   // the limit is a per-function attribute shared by every handle: set it per launch
   if (L.smooth_smem > 48 * 1024)
-    FG_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smooth_smem));
+    ensure_smem(k, L.smooth_smem);
   launch_clustered(k, L.ngroups * L.cluster, L.smooth_threads, L.smooth_smem, L.cluster, s,
                    (const int32_t*)L.grows.p, (const int32_t*)L.Ain.rp.p, (const int32_t*)L.Ain.ci.p,
                    (const T*)L.Ain.v.p, aorp, (const int32_t*)L.Aout.ci.p, (const T*)L.Aout.v.p,
@@ -1047,7 +1047,7 @@ void plan_smoother(Ctx& c, Level<T>& L) {
     for (int post = 0; post < 2; post++) {
       auto k = post ? smooth_reg_kernel<T, true, kRegRow> : smooth_reg_kernel<T, false, kRegRow>;
       if (L.smooth_smem > 48 * 1024)
-        FG_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smooth_smem));
+        ensure_smem(k, L.smooth_smem);
       int nb = 0;
       FG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, L.smooth_threads, L.smooth_smem));
       per_sm = post ? std::min(per_sm, nb) : nb;
@@ -1076,7 +1076,7 @@ void plan_smoother(Ctx& c, Level<T>& L) {
       bool fits = true;
       for (int post = 0; post < 2 && fits; post++) {
         CregSmoothFn<T> k = pick_creg_kernel<T>(post != 0, S, K);
-        if (sm > 48 * 1024) FG_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        if (sm > 48 * 1024) ensure_smem(k, sm);
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3((unsigned)(L.ngroups * C));
         cfg.blockDim = dim3((unsigned)thr);
@@ -1121,7 +1121,7 @@ void plan_smoother(Ctx& c, Level<T>& L) {
     bool fits = true;
     for (int post = 0; post < 2 && fits; post++) {
       ClusterSmoothFn<T> k = pick_cluster_kernel<T>(post != 0, st, S);
-      if (sm > 48 * 1024) FG_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      if (sm > 48 * 1024) ensure_smem(k, sm);
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3((unsigned)(L.ngroups * C));
       cfg.blockDim = dim3((unsigned)thr);

@@ -121,6 +121,15 @@ inline int grid_for(int64_t n, int block) {
   return (int)g;
 }
 
+// Raises a kernel's dynamic shared memory limit to at least `bytes` on the current
+// device.  The runtime call is slow (about a millisecond on GB300), so the largest
+// value set per (device, kernel) is remembered and the call is made only to raise it.
+void ensure_dynamic_smem(const void* func, size_t bytes);
+template <class F>
+inline void ensure_smem(F* func, size_t bytes) {
+  if (bytes > 48 * 1024) ensure_dynamic_smem(reinterpret_cast<const void*>(func), bytes);
+}
+
 // Host round trips of the setup (counted for its phase timer).
 extern std::atomic<int64_t> g_host_syncs;
 

@@ -1,8 +1,24 @@
 // primitives.cu -- scans, reductions and segmented sorts written for this library
 // (no Thrust/CUB on the product path).
+#include <map>
+#include <mutex>
+
 #include "common.cuh"
 
 namespace femgpu {
+
+void ensure_dynamic_smem(const void* func, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void*>, size_t> set;
+  int dev = 0;
+  FG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& cur = set[{dev, func}];
+  if (bytes <= cur) return;
+  FG_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  cur = bytes;
+}
+
 
 namespace {
 
