@@ -166,6 +166,11 @@ void random_mis(Ctx& c, int n, const int32_t* xadj, const int32_t* adj, int k, D
   FG_LAUNCH(mis_randoms_kernel, 128, 256, 0, s, n, (n + 32767) / 32768, randoms.p, dseeds.p);
   FG_LAUNCH(mis_first_init_kernel, grid_for(n, 256), 256, 0, s, n, randoms.p, k0.p);
   pt.mark("mis init");
+  // Rounds are enqueued in batches and the flag of a batch's last round is read once:
+  // a round after the one that completes the set changes nothing (decided nodes keep
+  // their state), so the extra rounds only cost time.  Small levels, where a host
+  // round trip costs more than a round, take larger batches.
+  const int batch = n < (1 << 18) ? 4 : 2;
   for (int round = 0;; round++) {
     FG_REQUIRE(round < kCap, FEMGPU_ERR_LIMIT, "randomized MIS did not complete");
     if (round > 0) FG_LAUNCH(mis_init_kernel, grid_for(n, 256), 256, 0, s, n, randoms.p, k0.p, mis.p);
@@ -176,8 +181,9 @@ void random_mis(Ctx& c, int n, const int32_t* xadj, const int32_t* adj, int k, D
       std::swap(ki, ko);
     }
     if (ki != k0.p) std::swap(k0.p, k1.p);  // keep k0 as the next round's input
+    if ((round + 1) % batch != 0) continue;
     if (read_scalar(flag.p, s) == 0) break;
-    pt.mark("mis round");
+    pt.mark("mis rounds");
   }
 }
 
@@ -399,9 +405,14 @@ void aggregate(Ctx& c, int n, const int32_t* xadj, const int32_t* adj, int depth
   bool first = true;
   for (int loop = 0;; loop++) {
     FG_REQUIRE(loop < kCap, FEMGPU_ERR_LIMIT, "aggregation did not complete");
-    counters.zero();
-    FG_LAUNCH(allocate_kernel, grid_for(n, 256), 256, 0, s, n, xadj, adj, part.p, pout.p, aggregated.p, counters.p);
-    std::swap(part.p, pout.p);
+    // two passes per host read: a pass after the one that leaves no node unallocated
+    // changes nothing, and the counters describe the second pass
+    for (int pass = 0; pass < 2; pass++) {
+      counters.zero();
+      FG_LAUNCH(allocate_kernel, grid_for(n, 256), 256, 0, s, n, xadj, adj, part.p, pout.p, aggregated.p,
+                counters.p);
+      std::swap(part.p, pout.p);
+    }
     int32_t h[2];
     counters.download(h, 2);
     FG_CUDA(cudaStreamSynchronize(s));

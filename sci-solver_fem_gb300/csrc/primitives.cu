@@ -112,7 +112,16 @@ __global__ void reduce_max_kernel(const int32_t* a, int64_t n, int32_t* out) {
     m = max(m, a[i]);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+  // one atomic per block
+  __shared__ int32_t wm[32];
+  if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    m = threadIdx.x < (blockDim.x >> 5) ? wm[threadIdx.x] : INT32_MIN;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (threadIdx.x == 0) atomicMax(out, m);
+  }
 }
 
 __global__ void count_equal_kernel(const int32_t* a, int64_t n, int32_t v, unsigned long long* out) {
@@ -121,7 +130,16 @@ __global__ void count_equal_kernel(const int32_t* a, int64_t n, int32_t v, unsig
     c += (a[i] == v);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-  if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, (unsigned long long)c);
+  // one atomic per block
+  __shared__ unsigned wc[32];
+  if ((threadIdx.x & 31) == 0) wc[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    c = threadIdx.x < (blockDim.x >> 5) ? wc[threadIdx.x] : 0u;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if (threadIdx.x == 0 && c) atomicAdd(out, (unsigned long long)c);
+  }
 }
 
 __global__ void fill_kernel(int32_t* a, int64_t n, int32_t v) {
