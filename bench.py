@@ -252,6 +252,16 @@ def main():
                           "algorithmic_bytes": kbytes, "ms": round(kms, 4)})
     roofline = max(rooflines, key=lambda r: r["ms"])
 
+    # final error of the timed solve against an FP64-hierarchy PCG solved to 1e-12
+    x_mixed = d_x.cpu().numpy()
+    ref = femgpu.Solver(solverType=1, tolerance=1e-12, maxIters=2000, flexibleCG=1, seed=1, precision=1,
+                        device=local)
+    ref.set_matrix_csr(rp, ci, s.matrix()[2])
+    ref.setup()
+    x_ref, st_ref = ref.solve(b, np.zeros(n))
+    final_error = float(np.linalg.norm(x_mixed - x_ref) / np.linalg.norm(x_ref))
+    ref.close()
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = len(os.sched_getaffinity(0))
@@ -270,6 +280,7 @@ def main():
                           "l2": "inputs larger than L2 (A: %.0f MB)" % (12 * nnz / 1e6)},
                "pcg_iterations": iters[-1], "relres": relres, "setup_ms": float(np.mean(setup_ms)),
                "solve_ms": float(np.mean(solve_ms)), "assembly_ms": assembly_ms,
+               "error_vs_fp64_1e-12": final_error, "fp64_1e-12_iterations": st_ref["iterations"],
                "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "rooflines": rooflines,
                "cpu_baseline": cpu,
                "clocks": clk}

@@ -145,6 +145,20 @@ femgpu_status femgpu_solve(femgpu_handle h, const double* b, double* x, femgpu_s
 femgpu_status femgpu_solve_device(femgpu_handle h, const double* d_b, double* d_x,
                                   femgpu_solve_stats* stats);
 
+/* Gradient of a loss L(u) with respect to theta_e = log c_e, the per-element
+ * log-coefficients of the operator assembled by femgpu_assemble (A(theta) u = b with
+ * the Dirichlet rows of femgpu_set_dirichlet eliminated): solves the adjoint system
+ * A lambda = dL/du (its Dirichlet entries set to 0) with the current hierarchy and PCG
+ * options, then dL/dtheta_e = -c_e lambda_e^T K_e u_e with K_e the element stiffness
+ * for c_e = 1 (the mass term does not depend on theta).  Host arrays: dLdu and u
+ * (nverts, u = the forward solution), dLdtheta (nelems).  stats may be NULL.
+ * No reference counterpart: the reference computes no gradients. */
+femgpu_status femgpu_adjoint_grad(femgpu_handle h, const double* dLdu, const double* u, double* dLdtheta,
+                                 femgpu_solve_stats* stats);
+/* Same with device pointers on the handle's stream. */
+femgpu_status femgpu_adjoint_grad_device(femgpu_handle h, const double* d_dLdu, const double* d_u,
+                                        double* d_grad, femgpu_solve_stats* stats);
+
 /* y = A x with the level-0 FP64 operator, device pointers, original numbering.
  * Replaces cusp::multiply(Ahyb_d_CG, ...) in cgcycle.cu:24,38. */
 femgpu_status femgpu_spmv_device(femgpu_handle h, const double* d_x, double* d_y);

@@ -294,6 +294,8 @@ femgpu_status femgpu_assemble(femgpu_handle h, const double* coef, double lambda
     invalidate_hierarchy(*h);
     assemble_operator(*h, coef, lambda_mass);
     h->has_matrix = true;
+    h->assembled_from_mesh = true;
+    h->dmask.release();
     FG_CUDA(cudaStreamSynchronize(h->stream));
   });
 }
@@ -330,6 +332,7 @@ femgpu_status femgpu_set_matrix_csr(femgpu_handle h, int64_t n, const int32_t* r
       }
     }
     invalidate_hierarchy(*h);
+    h->assembled_from_mesh = false;
     cudaStream_t s = h->stream;
     DCsr<double>& A = h->A;
     A.n = A.m = (int)n;
@@ -392,6 +395,62 @@ femgpu_status femgpu_solve(femgpu_handle h, const double* b, double* x, femgpu_s
     dx.upload(x, n);
     result = femgpu_solve_device(h, db.p, dx.p, stats);
     dx.download(x, n);
+    FG_CUDA(cudaStreamSynchronize(h->stream));
+  });
+  return st != FEMGPU_OK ? st : result;
+}
+
+femgpu_status femgpu_adjoint_grad_device(femgpu_handle h, const double* d_dLdu, const double* d_u,
+                                        double* d_grad, femgpu_solve_stats* stats) {
+  if (!h || !d_dLdu || !d_u || !d_grad) return FEMGPU_ERR_INVALID;
+  femgpu_status result = FEMGPU_OK;
+  femgpu_status st = guard(h, [&] {
+    FG_REQUIRE(h->has_mesh && h->has_matrix && h->assembled_from_mesh, FEMGPU_ERR_NOT_READY,
+               "the adjoint gradient needs an operator assembled from the mesh (femgpu_assemble)");
+    if (!h->has_hierarchy) amg_setup(*h);
+    const int64_t n = h->A.n;
+    cudaStream_t s = h->stream;
+    DBuf<double> g(n, s), lam(n, s);
+    zero_dirichlet_rows(*h, d_dLdu, g.p);  // u is fixed on Dirichlet rows
+    lam.zero();
+    cudaEvent_t e0, e1;
+    FG_CUDA(cudaEventCreate(&e0));
+    FG_CUDA(cudaEventCreate(&e1));
+    FG_CUDA(cudaEventRecord(e0, s));
+    SolveResult r = amg_solve_device(*h, g.p, lam.p);  // A is symmetric: A^T lambda = dL/du
+    element_log_coef_gradient(*h, lam.p, d_u, d_grad);
+    FG_CUDA(cudaEventRecord(e1, s));
+    FG_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    FG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (stats) {
+      stats->iterations = r.iterations;
+      stats->relative_residual = r.relres;
+      stats->setup_ms = h->setup_ms;
+      stats->solve_ms = ms;
+      stats->num_levels = h->H ? h->H->num_levels : 0;
+    }
+    result = r.status;
+    if (r.status == FEMGPU_ERR_NOT_CONVERGED) h->last_error = "adjoint PCG reached maxIters";
+    if (r.status == FEMGPU_ERR_BREAKDOWN) h->last_error = "adjoint PCG breakdown (non-positive curvature or NaN)";
+  });
+  return st != FEMGPU_OK ? st : result;
+}
+
+femgpu_status femgpu_adjoint_grad(femgpu_handle h, const double* dLdu, const double* u, double* dLdtheta,
+                                 femgpu_solve_stats* stats) {
+  if (!h || !dLdu || !u || !dLdtheta) return FEMGPU_ERR_INVALID;
+  femgpu_status result = FEMGPU_OK;
+  femgpu_status st = guard(h, [&] {
+    FG_REQUIRE(h->has_mesh, FEMGPU_ERR_NOT_READY, "femgpu_set_mesh first");
+    const int64_t n = h->A.n, ne = h->mesh.ne;
+    DBuf<double> dg(n, h->stream), du(n, h->stream), dt(ne, h->stream);
+    dg.upload(dLdu, n);
+    du.upload(u, n);
+    result = femgpu_adjoint_grad_device(h, dg.p, du.p, dt.p, stats);
+    dt.download(dLdtheta, ne);
     FG_CUDA(cudaStreamSynchronize(h->stream));
   });
   return st != FEMGPU_OK ? st : result;

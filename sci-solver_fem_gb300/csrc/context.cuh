@@ -114,6 +114,9 @@ struct Ctx {
 
   Mesh mesh;
   bool has_mesh = false;
+  DBuf<double> coef;             // per-element coefficients of the last femgpu_assemble (empty: labels / 1)
+  DBuf<uint8_t> dmask;           // Dirichlet mask of the last femgpu_set_dirichlet (empty: none)
+  bool assembled_from_mesh = false;
   DCsr<double> A;                // level-0 operator, original numbering, FP64
   DBuf<int32_t> gxadj, gadj;     // level-0 aggregation graph
   int64_t graph_nnz = 0;
@@ -152,6 +155,10 @@ void load_vector(Ctx& c, const double* f_host, double* b_host);
 // and `fsum`, one double per element each); enqueued on c.stream, allocates nothing.
 void load_vector_enqueue(Ctx& c, const double* d_f, double* d_b, double* scale, double* fsum);
 void apply_dirichlet(Ctx& c, const uint8_t* mask_host);
+// out = in with the Dirichlet rows set to zero (n = rows of the operator).
+void zero_dirichlet_rows(Ctx& c, const double* d_in, double* d_out);
+// dL/dtheta_e = -c_e lambda_e^T K_e u_e for theta_e = log c_e (per element, device arrays).
+void element_log_coef_gradient(Ctx& c, const double* d_lam, const double* d_u, double* d_grad);
 
 // amg_setup.cu
 void amg_setup(Ctx& c);

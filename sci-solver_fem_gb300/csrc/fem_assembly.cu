@@ -125,52 +125,59 @@ __global__ void graph_from_pattern_kernel(const int32_t* rowptr, const int32_t* 
 }
 
 // ---- assembly --------------------------------------------------------------------
+// Vertex coordinates, volume and P1 basis gradients g[a] of tetrahedron e (the
+// cofactor inverse of perform_element_loop_3D.cuh:525-583, terms in its order).
+__device__ __forceinline__ void tet_basis(const double* __restrict__ xyz, const int32_t* __restrict__ conn,
+                                          int64_t e, double x[4], double y[4], double z[4], double& vol,
+                                          double g[4][3]) {
+  int id[4];
+#pragma unroll
+  for (int a = 0; a < 4; a++) {
+    id[a] = conn[e * 4 + a];
+    x[a] = xyz[(int64_t)id[a] * 3];
+    y[a] = xyz[(int64_t)id[a] * 3 + 1];
+    z[a] = xyz[(int64_t)id[a] * 3 + 2];
+  }
+  double a1 = x[1] - x[3], a2 = y[1] - y[3], a3 = z[1] - z[3];
+  double b1 = x[2] - x[3], b2 = y[2] - y[3], b3 = z[2] - z[3];
+  double c1 = x[0] - x[3], c2 = y[0] - y[3], c3 = z[0] - z[3];
+  vol = fabs(c1 * (a2 * b3 - a3 * b2) + c2 * (a3 * b1 - a1 * b3) + c3 * (a1 * b2 - a2 * b1)) / 6.0;
+  double m[16];
+#pragma unroll
+  for (int r = 0; r < 4; r++) {
+    m[r * 4 + 0] = x[r];
+    m[r * 4 + 1] = y[r];
+    m[r * 4 + 2] = z[r];
+    m[r * 4 + 3] = 1.0;
+  }
+  double det = m[c_det[0][0]] * m[c_det[0][1]] * m[c_det[0][2]] * m[c_det[0][3]];
+#pragma unroll
+  for (int t = 1; t < 24; t++) {
+    double p = m[c_det[t][0]] * m[c_det[t][1]] * m[c_det[t][2]] * m[c_det[t][3]];
+    det = t < 12 ? det + p : det - p;
+  }
+#pragma unroll
+  for (int kk = 0; kk < 4; kk++) {
+#pragma unroll
+    for (int mm = 0; mm < 3; mm++) {
+      const unsigned char(*T)[3] = c_cof[mm * 4 + kk];
+      double s = m[T[0][0]] * m[T[0][1]] * m[T[0][2]];
+      s = s + m[T[1][0]] * m[T[1][1]] * m[T[1][2]];
+      s = s + m[T[2][0]] * m[T[2][1]] * m[T[2][2]];
+      s = s - m[T[3][0]] * m[T[3][1]] * m[T[3][2]];
+      s = s - m[T[4][0]] * m[T[4][1]] * m[T[4][2]];
+      s = s - m[T[5][0]] * m[T[5][1]] * m[T[5][2]];
+      g[kk][mm] = s / det;
+    }
+  }
+}
+
 __global__ void element3d_kernel(const double* __restrict__ xyz, const int32_t* __restrict__ conn,
                                  const int32_t* __restrict__ labels, const double* __restrict__ coef, int64_t ne,
                                  double lambda, double* __restrict__ ev) {
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
-    int id[4];
-    double x[4], y[4], z[4];
-#pragma unroll
-    for (int a = 0; a < 4; a++) {
-      id[a] = conn[e * 4 + a];
-      x[a] = xyz[(int64_t)id[a] * 3];
-      y[a] = xyz[(int64_t)id[a] * 3 + 1];
-      z[a] = xyz[(int64_t)id[a] * 3 + 2];
-    }
-    double a1 = x[1] - x[3], a2 = y[1] - y[3], a3 = z[1] - z[3];
-    double b1 = x[2] - x[3], b2 = y[2] - y[3], b3 = z[2] - z[3];
-    double c1 = x[0] - x[3], c2 = y[0] - y[3], c3 = z[0] - z[3];
-    double vol = fabs(c1 * (a2 * b3 - a3 * b2) + c2 * (a3 * b1 - a1 * b3) + c3 * (a1 * b2 - a2 * b1)) / 6.0;
-    double m[16];
-#pragma unroll
-    for (int r = 0; r < 4; r++) {
-      m[r * 4 + 0] = x[r];
-      m[r * 4 + 1] = y[r];
-      m[r * 4 + 2] = z[r];
-      m[r * 4 + 3] = 1.0;
-    }
-    double det = m[c_det[0][0]] * m[c_det[0][1]] * m[c_det[0][2]] * m[c_det[0][3]];
-#pragma unroll
-    for (int t = 1; t < 24; t++) {
-      double p = m[c_det[t][0]] * m[c_det[t][1]] * m[c_det[t][2]] * m[c_det[t][3]];
-      det = t < 12 ? det + p : det - p;
-    }
-    double g[4][3];
-#pragma unroll
-    for (int kk = 0; kk < 4; kk++) {
-#pragma unroll
-      for (int mm = 0; mm < 3; mm++) {
-        const unsigned char(*T)[3] = c_cof[mm * 4 + kk];
-        double s = m[T[0][0]] * m[T[0][1]] * m[T[0][2]];
-        s = s + m[T[1][0]] * m[T[1][1]] * m[T[1][2]];
-        s = s + m[T[2][0]] * m[T[2][1]] * m[T[2][2]];
-        s = s - m[T[3][0]] * m[T[3][1]] * m[T[3][2]];
-        s = s - m[T[4][0]] * m[T[4][1]] * m[T[4][2]];
-        s = s - m[T[5][0]] * m[T[5][1]] * m[T[5][2]];
-        g[kk][mm] = s / det;
-      }
-    }
+    double x[4], y[4], z[4], vol, g[4][3];
+    tet_basis(xyz, conn, e, x, y, z, vol, g);
     const double X1 = x[0], Y1 = y[0], Z1 = z[0], X2 = x[1], Y2 = y[1], Z2 = z[1];
     const double X3 = x[2], Y3 = y[2], Z3 = z[2], X4 = x[3], Y4 = y[3], Z4 = z[3];
     double mdet = 0.125 * ((-X1 + X2) * (-Y1 + Y3) * (-Z1 + Z4) + (-Y1 + Y2) * (-Z1 + Z3) * (-X1 + X4) +
@@ -317,6 +324,70 @@ __global__ void dirichlet_kernel(const int32_t* rowptr, const int32_t* cols, dou
   }
 }
 
+// dL/dtheta_e = -c_e * vol_e * grad(lambda)_e . grad(u)_e for P1 tetrahedra: the
+// derivative of lambda^T A(theta) u through the stiffness term c_e K_e with
+// c_e = exp(theta_e) (the mass term does not depend on theta).
+__global__ void grad3d_kernel(const double* __restrict__ xyz, const int32_t* __restrict__ conn,
+                              const int32_t* __restrict__ labels, const double* __restrict__ coef, int64_t ne,
+                              const double* __restrict__ lam, const double* __restrict__ u,
+                              double* __restrict__ grad) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
+    double x[4], y[4], z[4], vol, g[4][3];
+    tet_basis(xyz, conn, e, x, y, z, vol, g);
+    double gl[3] = {0.0, 0.0, 0.0}, gu[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+      const int v = conn[e * 4 + a];
+      const double la = lam[v], ua = u[v];
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        gl[d] = fma(la, g[a][d], gl[d]);
+        gu[d] = fma(ua, g[a][d], gu[d]);
+      }
+    }
+    const double co = coef ? coef[e] : (labels ? label_coef(labels[e]) : 1.0);
+    grad[e] = -co * vol * (gl[0] * gu[0] + gl[1] * gu[1] + gl[2] * gu[2]);
+  }
+}
+
+// The same for P1 triangles (basis gradients from the 3x3 cofactor inverse).
+__global__ void grad2d_kernel(const double* __restrict__ xyz, const int32_t* __restrict__ conn,
+                              const double* __restrict__ coef, int64_t ne, const double* __restrict__ lam,
+                              const double* __restrict__ u, double* __restrict__ grad) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
+    double x[3], y[3], la[3], ua[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      const int v = conn[e * 3 + a];
+      x[a] = xyz[(int64_t)v * 3];
+      y[a] = xyz[(int64_t)v * 3 + 1];
+      la[a] = lam[v];
+      ua[a] = u[v];
+    }
+    const double area = fabs(x[0] * y[2] - x[0] * y[1] + x[1] * y[0] - x[1] * y[2] + x[2] * y[1] - x[2] * y[0]) / 2.0;
+    const double det = x[0] * y[1] + x[1] * y[2] + x[2] * y[0] - x[0] * y[2] - x[2] * y[1] - x[1] * y[0];
+    // gradient of basis a: ((y[b] - y[c]) / det, (x[c] - x[b]) / det) with (a, b, c) cyclic
+    double gl[2] = {0.0, 0.0}, gu[2] = {0.0, 0.0};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      const int b = (a + 1) % 3, c = (a + 2) % 3;
+      const double gx = (y[b] - y[c]) / det, gy = (x[c] - x[b]) / det;
+      gl[0] = fma(la[a], gx, gl[0]);
+      gl[1] = fma(la[a], gy, gl[1]);
+      gu[0] = fma(ua[a], gx, gu[0]);
+      gu[1] = fma(ua[a], gy, gu[1]);
+    }
+    const double co = coef ? coef[e] : 1.0;
+    grad[e] = -co * area * (gl[0] * gu[0] + gl[1] * gu[1]);
+  }
+}
+
+__global__ void mask_rows_kernel(int n, const uint8_t* __restrict__ mask, const double* __restrict__ in,
+                                 double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (mask && mask[i]) ? 0.0 : in[i];
+}
+
 }  // namespace
 
 void build_mesh_pattern(Ctx& c) {
@@ -383,7 +454,8 @@ void assemble_operator(Ctx& c, const double* coef_host, double lambda) {
     }
     FG_CUDA(cudaMemcpyToSymbolAsync(c_tri_q, q, sizeof(q), 0, cudaMemcpyHostToDevice, s));
   }
-  DBuf<double> coef;
+  DBuf<double>& coef = c.coef;  // kept for the adjoint gradient
+  coef.release();
   if (coef_host) {
     coef.alloc(ne, s);
     coef.upload(coef_host, ne);
@@ -421,9 +493,26 @@ void load_vector_enqueue(Ctx& c, const double* d_f, double* d_b, double* scale, 
             M.k, d_b);
 }
 
+void zero_dirichlet_rows(Ctx& c, const double* d_in, double* d_out) {
+  const int n = c.A.n;
+  FG_LAUNCH(mask_rows_kernel, grid_for(n, 256), 256, 0, c.stream, n, c.dmask.n ? c.dmask.p : nullptr, d_in, d_out);
+}
+
+void element_log_coef_gradient(Ctx& c, const double* d_lam, const double* d_u, double* d_grad) {
+  Mesh& M = c.mesh;
+  const double* coef = c.coef.n ? c.coef.p : nullptr;
+  if (M.k == 4)
+    FG_LAUNCH(grad3d_kernel, grid_for(M.ne, 128), 128, 0, c.stream, M.xyz.p, M.conn.p,
+              M.has_labels ? M.labels.p : nullptr, coef, M.ne, d_lam, d_u, d_grad);
+  else
+    FG_LAUNCH(grad2d_kernel, grid_for(M.ne, 128), 128, 0, c.stream, M.xyz.p, M.conn.p, coef, M.ne, d_lam, d_u,
+              d_grad);
+}
+
 void apply_dirichlet(Ctx& c, const uint8_t* mask_host) {
   cudaStream_t s = c.stream;
-  DBuf<uint8_t> mask(c.A.n, s);
+  DBuf<uint8_t>& mask = c.dmask;  // kept for the adjoint right-hand side
+  mask.alloc(c.A.n, s);
   mask.upload(mask_host, c.A.n);
   FG_LAUNCH(dirichlet_kernel, grid_for(c.A.n, 256), 256, 0, s, c.A.rp.p, c.A.ci.p, c.A.v.p, mask.p, c.A.n);
   FG_CUDA(cudaStreamSynchronize(s));

@@ -25,7 +25,8 @@ EXPORTS = [
     "femgpu_set_mesh", "femgpu_assemble", "femgpu_load_vector", "femgpu_set_dirichlet", "femgpu_set_matrix_csr",
     "femgpu_setup", "femgpu_solve", "femgpu_solve_device", "femgpu_spmv_device", "femgpu_get_matrix",
     "femgpu_num_levels", "femgpu_get_level_info", "femgpu_level_get", "femgpu_vcycle", "femgpu_kernel_launches",
-    "femgpu_profile_kernel", "femgpu_load_vector_device_noalloc",
+    "femgpu_profile_kernel", "femgpu_load_vector_device_noalloc", "femgpu_adjoint_grad",
+    "femgpu_adjoint_grad_device",
     "femgpu_read_tetgen", "femgpu_read_ply", "femgpu_read_mat_sparse", "femgpu_read_mat_array",
     "femgpu_write_mat_array", "femgpu_write_vtk",
 ]
@@ -97,6 +98,8 @@ def lib():
     L.femgpu_solve_device.argtypes = [_vp, _vp, _vp, C.POINTER(SolveStats)]
     L.femgpu_spmv_device.argtypes = [_vp, _vp, _vp]
     L.femgpu_load_vector_device_noalloc.argtypes = [_vp, _vp, _vp]
+    L.femgpu_adjoint_grad.argtypes = [_vp, _f64p, _f64p, _f64p, C.POINTER(SolveStats)]
+    L.femgpu_adjoint_grad_device.argtypes = [_vp, _vp, _vp, _vp, C.POINTER(SolveStats)]
     L.femgpu_get_matrix.argtypes = [_vp, _pi64, _pi64, _vp, _vp, _vp]
     L.femgpu_num_levels.argtypes = [_vp, C.POINTER(C.c_int)]
     L.femgpu_get_level_info.argtypes = [_vp, C.c_int, C.POINTER(LevelInfo)]
@@ -173,6 +176,7 @@ class Solver:
         _check(lib().femgpu_set_mesh(self.h, dim, xyz.shape[0], xyz.ravel(), conn.shape[0], conn.ravel(),
                                      _ptr(labels)), self.h)
         self.n = xyz.shape[0]
+        self.nelems = conn.shape[0]
         self.dim = dim
         self._labels_keep = labels
 
@@ -268,6 +272,25 @@ class Solver:
         ms, nb = C.c_double(), C.c_double()
         _check(lib().femgpu_profile_kernel(self.h, which, reps, C.byref(ms), C.byref(nb)), self.h)
         return ms.value, nb.value
+
+    def adjoint_grad(self, dLdu, u, check=True):
+        """dL/dtheta per element for theta = log(coefficients) (host arrays)."""
+        ne = self.nelems
+        out = np.zeros(ne)
+        st = SolveStats()
+        status = lib().femgpu_adjoint_grad(self.h, np.ascontiguousarray(dLdu, dtype=np.float64),
+                                           np.ascontiguousarray(u, dtype=np.float64), out, C.byref(st))
+        if check and status != 0:
+            _check(status, self.h)
+        return out, dict(status=status, iterations=st.iterations, relres=st.relative_residual,
+                         solve_ms=st.solve_ms)
+
+    def adjoint_grad_device(self, dLdu_ptr: int, u_ptr: int, grad_ptr: int):
+        """Device pointers on the handle's stream."""
+        st = SolveStats()
+        _check(lib().femgpu_adjoint_grad_device(self.h, _vp(dLdu_ptr), _vp(u_ptr), _vp(grad_ptr), C.byref(st)),
+               self.h)
+        return dict(iterations=st.iterations, relres=st.relative_residual, solve_ms=st.solve_ms)
 
     def spmv_device(self, x_ptr: int, y_ptr: int):
         _check(lib().femgpu_spmv_device(self.h, _vp(x_ptr), _vp(y_ptr)), self.h)
