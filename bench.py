@@ -11,6 +11,12 @@ e2e = the same through femgpu_setup + femgpu_solve with host b/x buffers.
 --precision mixed (default): FP32 hierarchy inside the FP64 outer PCG;
 --precision fp64: the same code with an FP64 hierarchy.
 --impl reference: the reference algorithm's CPU restatement (oracle) on host cores.
+--workload batched: 64^3 mesh with 64 seeded right-hand sides solved with one hierarchy
+  (femgpu_solve_multi); reports right-hand-side DOF/s.
+--workload differentiation: 96^3 mesh, theta_e = log kappa_e ~ N(0,1), loss over a 1%
+  vertex subset; forward solve + adjoint gradient (femgpu_adjoint_grad) timed, gradient
+  compared with the FP64-hierarchy gradient solved to 1e-12.
+Only the default workload is the headline line.
 """
 import argparse
 import json
@@ -107,6 +113,97 @@ def cpu_baseline(n_sample, sigma, threads):
     return free / dt, dt, st
 
 
+def run_batched(args):
+    """64^3 mesh, 64 right-hand sides, one hierarchy: setup + 64 PCG solves per step."""
+    import torch
+    import femgpu
+    xyz, conn, kappa, f, mask = problem(64, 1.0)
+    n = xyz.shape[0]
+    free = int(n - mask.sum())
+    s = femgpu.Solver(solverType=1, tolerance=1e-8, maxIters=500, flexibleCG=1, seed=1)
+    s.set_mesh(xyz, conn)
+    s.assemble(kappa, 0.0)
+    s.set_dirichlet(mask)
+    rng = np.random.default_rng(6)
+    k = 64
+    B = np.stack([np.where(mask.astype(bool), 0.0, s.load_vector(rng.uniform(-1.0, 1.0, n))) for _ in range(k)])
+    dB = torch.from_numpy(B).cuda()  # k x n: column j of the solve is row j here
+    dX = torch.zeros_like(dB)
+    times, iters = [], []
+    for step in range(args.warmup + args.steps):
+        dX.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.setup()
+        st = s.solve_multi_device(k, dB.data_ptr(), n, dX.data_ptr(), n)
+        torch.cuda.synchronize()
+        if step >= args.warmup:
+            times.append(time.perf_counter() - t0)
+            iters.append(st["iterations"])
+    dt = float(np.mean(times))
+    out = {"metric": "batched AMG-PCG right-hand-side DOF/s (64 RHS, one hierarchy)", "value": k * free / dt,
+           "unit": "DOF*RHS/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt,
+           "higher_is_better": True, "dtype": "f64+f32", "data": "synthetic",
+           "config": {"workload": "poisson3d_kuhn_64^3_64rhs", "dofs": n, "free_dofs": free, "nrhs": k},
+           "pcg_iterations_total": int(np.mean(iters)), "relres_max": st["relres"]}
+    print(json.dumps(out))
+
+
+def run_differentiation(args):
+    """96^3 mesh: forward solve + adjoint gradient per step; gradient vs an FP64 one."""
+    import torch
+    import femgpu
+    from femgpu import meshes
+    xyz, conn = meshes.kuhn_cube(96)
+    n, ne = xyz.shape[0], conn.shape[0]
+    mask = (xyz[:, 2] == 0.0).astype(np.uint8)
+    rng = np.random.default_rng(9)
+    theta = rng.standard_normal(ne)
+    S = np.random.default_rng(10).choice(n, n // 100, replace=False)
+    theta_obs = np.random.default_rng(11).standard_normal(ne)
+    f = np.random.default_rng(5).uniform(-1.0, 1.0, n)
+
+    def forward(th, precision, tol):
+        s = femgpu.Solver(solverType=1, tolerance=tol, maxIters=2000, flexibleCG=1, seed=1, precision=precision)
+        s.set_mesh(xyz, conn)
+        b = np.where(mask.astype(bool), 0.0, s.load_vector(f))
+        s.assemble(np.exp(th), 0.0)
+        s.set_dirichlet(mask)
+        s.setup()
+        u, st = s.solve(b)
+        return s, u
+
+    _, u_obs = forward(theta_obs, 1, 1e-12)
+    times, fwd_ms, adj_ms = [], [], []
+    for step in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s, u = forward(theta, 0, 1e-8)
+        t1 = time.perf_counter()
+        r = np.zeros(n)
+        r[S] = u[S] - u_obs[S]
+        g, st = s.adjoint_grad(r, u)
+        t2 = time.perf_counter()
+        if step >= args.warmup:
+            times.append(t2 - t0)
+            fwd_ms.append(1e3 * (t1 - t0))
+            adj_ms.append(1e3 * (t2 - t1))
+        s.close()
+    # FP64 hierarchy, 1e-12 forward and adjoint: the reference gradient
+    sr, ur = forward(theta, 1, 1e-12)
+    rr = np.zeros(n)
+    rr[S] = ur[S] - u_obs[S]
+    gr, _ = sr.adjoint_grad(rr, ur)
+    rel = float(np.linalg.norm(g - gr) / np.linalg.norm(gr))
+    out = {"metric": "forward + adjoint gradient wall time (96^3, mixed precision)",
+           "value": 1e3 * float(np.mean(times)), "unit": "ms", "higher_is_better": False, "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "data": "synthetic",
+           "config": {"workload": "poisson3d_kuhn_96^3_adjoint", "dofs": n, "elements": ne, "observed": len(S)},
+           "forward_ms": float(np.mean(fwd_ms)), "adjoint_ms": float(np.mean(adj_ms)),
+           "gradient_rel_error_vs_fp64_1e-12": rel}
+    print(json.dumps(out))
+
+
 def run_reference(args):
     """--impl reference: the reference's algorithm on the host cores (oracle port)."""
     rank = int(os.environ.get("RANK", "0"))
@@ -145,9 +242,16 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--cpu-sample", type=int, default=48)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="poisson", choices=["poisson", "batched", "differentiation"])
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload == "batched":
+        run_batched(args)
+        return
+    if args.workload == "differentiation":
+        run_differentiation(args)
         return
 
     import torch

@@ -141,6 +141,16 @@ femgpu_status femgpu_setup(femgpu_handle h);
  * (cgcycle.cu:6-69).  stats may be NULL. */
 femgpu_status femgpu_solve(femgpu_handle h, const double* b, double* x, femgpu_solve_stats* stats);
 
+/* nrhs right-hand sides with one hierarchy: column j of B (and of X, which holds the
+ * initial guesses) is nverts doubles at B + j * nverts (host arrays).  stats: summed
+ * iterations, largest relative residual, total solve time.  No reference counterpart
+ * (the reference solves one right-hand side per FEMSolver::solveFEM). */
+femgpu_status femgpu_solve_multi(femgpu_handle h, int nrhs, const double* B, double* X,
+                                 femgpu_solve_stats* stats);
+/* Same with device arrays and leading dimensions ldb, ldx >= nverts. */
+femgpu_status femgpu_solve_multi_device(femgpu_handle h, int nrhs, const double* d_B, int64_t ldb, double* d_X,
+                                       int64_t ldx, femgpu_solve_stats* stats);
+
 /* Same as femgpu_solve with device pointers on the handle's stream (no copies). */
 femgpu_status femgpu_solve_device(femgpu_handle h, const double* d_b, double* d_x,
                                   femgpu_solve_stats* stats);

@@ -3,6 +3,7 @@
 // Every entry point catches library errors and CUDA failures and turns them into
 // a status code (the reference calls exit() on bad input, gauss_seidel.cu:2060-2064;
 // tetmesh.cu:257-260); the message is kept on the handle (femgpu_last_error).
+#include <algorithm>
 #include <cstring>
 #include <functional>
 
@@ -395,6 +396,64 @@ femgpu_status femgpu_solve(femgpu_handle h, const double* b, double* x, femgpu_s
     dx.upload(x, n);
     result = femgpu_solve_device(h, db.p, dx.p, stats);
     dx.download(x, n);
+    FG_CUDA(cudaStreamSynchronize(h->stream));
+  });
+  return st != FEMGPU_OK ? st : result;
+}
+
+femgpu_status femgpu_solve_multi_device(femgpu_handle h, int nrhs, const double* d_B, int64_t ldb, double* d_X,
+                                       int64_t ldx, femgpu_solve_stats* stats) {
+  if (!h || !d_B || !d_X || nrhs < 0) return FEMGPU_ERR_INVALID;
+  femgpu_status result = FEMGPU_OK;
+  femgpu_status st = guard(h, [&] {
+    FG_REQUIRE(h->has_matrix, FEMGPU_ERR_NOT_READY, "no operator");
+    const int64_t n = h->A.n;
+    FG_REQUIRE(ldb >= n && ldx >= n, FEMGPU_ERR_INVALID, "leading dimension smaller than the rows");
+    if (!h->has_hierarchy) amg_setup(*h);
+    cudaEvent_t e0, e1;
+    FG_CUDA(cudaEventCreate(&e0));
+    FG_CUDA(cudaEventCreate(&e1));
+    FG_CUDA(cudaEventRecord(e0, h->stream));
+    int iters = 0;
+    double worst = 0.0;
+    for (int j = 0; j < nrhs; j++) {
+      // one hierarchy, one captured PCG loop, one column at a time
+      SolveResult r = amg_solve_device(*h, d_B + j * ldb, d_X + j * ldx);
+      iters += r.iterations;
+      worst = std::max(worst, r.relres);
+      if (r.status != FEMGPU_OK && result == FEMGPU_OK) result = r.status;
+    }
+    FG_CUDA(cudaEventRecord(e1, h->stream));
+    FG_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    FG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (stats) {
+      stats->iterations = iters;
+      stats->relative_residual = worst;
+      stats->setup_ms = h->setup_ms;
+      stats->solve_ms = ms;
+      stats->num_levels = h->H ? h->H->num_levels : 0;
+    }
+    if (result == FEMGPU_ERR_NOT_CONVERGED) h->last_error = "PCG reached maxIters on a right-hand side";
+    if (result == FEMGPU_ERR_BREAKDOWN) h->last_error = "PCG breakdown on a right-hand side";
+  });
+  return st != FEMGPU_OK ? st : result;
+}
+
+femgpu_status femgpu_solve_multi(femgpu_handle h, int nrhs, const double* B, double* X,
+                                 femgpu_solve_stats* stats) {
+  if (!h || !B || !X || nrhs < 0) return FEMGPU_ERR_INVALID;
+  femgpu_status result = FEMGPU_OK;
+  femgpu_status st = guard(h, [&] {
+    FG_REQUIRE(h->has_matrix, FEMGPU_ERR_NOT_READY, "no operator");
+    const int64_t n = h->A.n, total = n * (int64_t)nrhs;
+    DBuf<double> db(total, h->stream), dx(total, h->stream);
+    db.upload(B, total);
+    dx.upload(X, total);
+    result = femgpu_solve_multi_device(h, nrhs, db.p, n, dx.p, n, stats);
+    dx.download(X, total);
     FG_CUDA(cudaStreamSynchronize(h->stream));
   });
   return st != FEMGPU_OK ? st : result;

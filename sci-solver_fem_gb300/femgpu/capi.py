@@ -26,7 +26,7 @@ EXPORTS = [
     "femgpu_setup", "femgpu_solve", "femgpu_solve_device", "femgpu_spmv_device", "femgpu_get_matrix",
     "femgpu_num_levels", "femgpu_get_level_info", "femgpu_level_get", "femgpu_vcycle", "femgpu_kernel_launches",
     "femgpu_profile_kernel", "femgpu_load_vector_device_noalloc", "femgpu_adjoint_grad",
-    "femgpu_adjoint_grad_device",
+    "femgpu_adjoint_grad_device", "femgpu_solve_multi", "femgpu_solve_multi_device",
     "femgpu_read_tetgen", "femgpu_read_ply", "femgpu_read_mat_sparse", "femgpu_read_mat_array",
     "femgpu_write_mat_array", "femgpu_write_vtk",
 ]
@@ -99,6 +99,8 @@ def lib():
     L.femgpu_spmv_device.argtypes = [_vp, _vp, _vp]
     L.femgpu_load_vector_device_noalloc.argtypes = [_vp, _vp, _vp]
     L.femgpu_adjoint_grad.argtypes = [_vp, _f64p, _f64p, _f64p, C.POINTER(SolveStats)]
+    L.femgpu_solve_multi.argtypes = [_vp, C.c_int, _f64p, _f64p, C.POINTER(SolveStats)]
+    L.femgpu_solve_multi_device.argtypes = [_vp, C.c_int, _vp, _i64, _vp, _i64, C.POINTER(SolveStats)]
     L.femgpu_adjoint_grad_device.argtypes = [_vp, _vp, _vp, _vp, C.POINTER(SolveStats)]
     L.femgpu_get_matrix.argtypes = [_vp, _pi64, _pi64, _vp, _vp, _vp]
     L.femgpu_num_levels.argtypes = [_vp, C.POINTER(C.c_int)]
@@ -272,6 +274,27 @@ class Solver:
         ms, nb = C.c_double(), C.c_double()
         _check(lib().femgpu_profile_kernel(self.h, which, reps, C.byref(ms), C.byref(nb)), self.h)
         return ms.value, nb.value
+
+    def solve_multi(self, B, X0=None, check=True):
+        """Columns of B (n x k, host) with one hierarchy; returns X (n x k) and stats."""
+        B = np.asarray(B, dtype=np.float64)
+        k = B.shape[1]
+        Bc = np.ascontiguousarray(B.T)  # column j contiguous
+        Xc = np.zeros_like(Bc) if X0 is None else np.ascontiguousarray(np.asarray(X0, dtype=np.float64).T)
+        st = SolveStats()
+        status = lib().femgpu_solve_multi(self.h, k, Bc.ravel(), Xc.ravel(), C.byref(st))
+        if check and status != 0:
+            _check(status, self.h)
+        return Xc.T.copy(), dict(status=status, iterations=st.iterations, relres=st.relative_residual,
+                                 solve_ms=st.solve_ms)
+
+    def solve_multi_device(self, nrhs: int, b_ptr: int, ldb: int, x_ptr: int, ldx: int, check=True):
+        """Device arrays (column j at ptr + j * ld doubles) on the handle's stream."""
+        st = SolveStats()
+        status = lib().femgpu_solve_multi_device(self.h, nrhs, _vp(b_ptr), ldb, _vp(x_ptr), ldx, C.byref(st))
+        if check and status != 0:
+            _check(status, self.h)
+        return dict(status=status, iterations=st.iterations, relres=st.relative_residual, solve_ms=st.solve_ms)
 
     def adjoint_grad(self, dLdu, u, check=True):
         """dL/dtheta per element for theta = log(coefficients) (host arrays)."""
