@@ -1071,19 +1071,24 @@ void run_esc_sort(Ctx& c, EscArgs<T> a, int nrows_out, int ncols_out, DCsr<T>& o
   const int wgrid = std::min<int64_t>((nrows_out + kEscWarps - 1) / kEscWarps, 152 * 64);
   a.counts = ucnt.p;
   a.thread_cap = kThreadRowCap;
-  FG_LAUNCH((esc_thread_kernel<T, MODE, false>), grid_for(nrows_out, 128), 128, 0, s, a, items.p);
-  FG_LAUNCH((esc_warp_kernel<T, MODE, false>), wgrid, 32 * kEscWarps, wsm, s, a, items.p);
-  if (a.nbig > 0)
-    FG_LAUNCH((esc_block_kernel<T, MODE, false>), std::min(a.nbig, 152 * 2), kEscBlockThreads, bsm, s, a, items.p);
-  if (ad.nbig > 0) {
-    ad.counts = ucnt.p;
-    FG_LAUNCH((esc_dense_kernel<T, MODE, false>), dgrid, 256, dense_shared ? dsm : 0, s, ad, ncols_out, gacc.p,
-              gmark.p);
+  // a permuted row has no repeated column: its output length is its item count, so the
+  // counting pass is needed only for the prolongator
+  if (MODE != ESC_PERMUTE) {
+    FG_LAUNCH((esc_thread_kernel<T, MODE, false>), grid_for(nrows_out, 128), 128, 0, s, a, items.p);
+    FG_LAUNCH((esc_warp_kernel<T, MODE, false>), wgrid, 32 * kEscWarps, wsm, s, a, items.p);
+    if (a.nbig > 0)
+      FG_LAUNCH((esc_block_kernel<T, MODE, false>), std::min(a.nbig, 152 * 2), kEscBlockThreads, bsm, s, a,
+                items.p);
+    if (ad.nbig > 0) {
+      ad.counts = ucnt.p;
+      FG_LAUNCH((esc_dense_kernel<T, MODE, false>), dgrid, 256, dense_shared ? dsm : 0, s, ad, ncols_out, gacc.p,
+                gmark.p);
+    }
   }
   out.n = nrows_out;
   out.m = ncols_out;
   out.rp.alloc(nrows_out + 1, s);
-  out.nnz = exclusive_scan(ucnt.p, out.rp.p, nrows_out, s);
+  out.nnz = exclusive_scan(MODE == ESC_PERMUTE ? items.p : ucnt.p, out.rp.p, nrows_out, s);
   out.ci.alloc(out.nnz > 0 ? out.nnz : 1, s);
   out.v.alloc(out.nnz > 0 ? out.nnz : 1, s);
   a.orp = out.rp.p;
