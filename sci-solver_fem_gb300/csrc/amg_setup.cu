@@ -456,6 +456,96 @@ __global__ void member_degree_kernel(int n, const int32_t* members, const int32_
   if (q < n) deg[q] = xadj[members[q] + 1] - xadj[members[q]];
 }
 
+// Induced-graph rows by hashing: one warp per aggregate walks the flattened neighbour
+// lists of its members 32 entries at a time (flat index f of member q starts at
+// noff[q]), groups equal aggregate ids with __match_any_sync, inserts each new id once
+// into a shared-memory set and finally sorts the set, so a row holds the sorted distinct
+// neighbour aggregates (what sorting the candidate list and dropping duplicates gives).
+// An aggregate with more than kIndCap - 32 distinct neighbours sets *overflow.
+constexpr int kIndCap = 256;
+
+__device__ __forceinline__ unsigned induced_hash(unsigned b) { return (b * 2654435761u) >> 9; }
+
+__global__ void __launch_bounds__(256) induced_hash_kernel(int nagg, const int32_t* __restrict__ astart,
+                                                           const int32_t* __restrict__ members,
+                                                           const int32_t* __restrict__ noff,
+                                                           const int32_t* __restrict__ xadj,
+                                                           const int32_t* __restrict__ adj,
+                                                           const int32_t* __restrict__ fine, int32_t* tmp,
+                                                           int32_t* ucount, int32_t* overflow) {
+  __shared__ int32_t hk[8][kIndCap];
+  __shared__ int32_t sk[8][kIndCap];
+  __shared__ int s_cnt[8];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int a = blockIdx.x * 8 + w; a < nagg; a += gridDim.x * 8) {
+    for (int t = lane; t < kIndCap; t += 32) hk[w][t] = -1;
+    if (lane == 0) s_cnt[w] = 0;
+    __syncwarp();
+    const int q0 = astart[a], q1 = astart[a + 1];
+    const int f0 = noff[q0], f1 = noff[q1];
+    bool over = false;
+    for (int fb = f0; fb < f1 && !over; fb += 32) {
+      const int f = fb + lane;
+      int b = -1;
+      if (f < f1) {
+        int lo = q0, hi = q1 - 1;  // last member q with noff[q] <= f
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (noff[mid] <= f) lo = mid;
+          else hi = mid - 1;
+        }
+        const int i = members[lo];
+        b = fine[adj[xadj[i] + (f - noff[lo])]];
+        if (b == a) b = -1;
+      }
+      const unsigned peers = __match_any_sync(0xffffffffu, b);
+      if (b >= 0 && (__ffs(peers) - 1) == lane) {
+        unsigned slot = induced_hash((unsigned)b) & (kIndCap - 1);
+        for (int p = 0; p < kIndCap; p++) {
+          const int prev = atomicCAS(&hk[w][slot], -1, b);
+          if (prev == -1) {
+            atomicAdd(&s_cnt[w], 1);
+            break;
+          }
+          if (prev == b) break;
+          slot = (slot + 1) & (kIndCap - 1);
+        }
+      }
+      __syncwarp();
+      over = s_cnt[w] > kIndCap - 32;  // the next chunk might not fit
+    }
+    if (over) {
+      if (lane == 0) *overflow = 1;
+      continue;
+    }
+    // compact the set, pad to a power of two, sort
+    const int cnt = s_cnt[w];
+    int base = 0;
+    for (int t0 = 0; t0 < kIndCap; t0 += 32) {
+      const int key = hk[w][t0 + lane];
+      const unsigned m = __ballot_sync(0xffffffffu, key >= 0);
+      if (key >= 0) sk[w][base + __popc(m & ((1u << lane) - 1u))] = key;
+      base += __popc(m);
+    }
+    const int np2 = next_pow2(cnt < 2 ? 2 : cnt);
+    for (int t = cnt + lane; t < np2; t += 32) sk[w][t] = INT32_MAX;
+    __syncwarp();
+    bitonic_sort_shared(sk[w], np2, lane, 32, WarpSync());
+    for (int t = lane; t < cnt; t += 32) tmp[(int64_t)a * kIndCap + t] = sk[w][t];
+    if (lane == 0) ucount[a] = cnt;
+    __syncwarp();
+  }
+}
+
+// Rows of fixed stride `stride` in src to their offsets doff in dst, one warp per row.
+__global__ void compact_stride_kernel(int nseg, const int32_t* src, int stride, const int32_t* doff, int32_t* dst) {
+  const int lane = threadIdx.x & 31;
+  for (int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < nseg; k += (gridDim.x * blockDim.x) >> 5) {
+    const int len = doff[k + 1] - doff[k];
+    for (int t = lane; t < len; t += 32) dst[doff[k] + t] = src[(int64_t)k * stride + t];
+  }
+}
+
 // One thread per member node: the aggregates of its neighbours go to the node's slice
 // of its aggregate's candidate list (its own aggregate as INT32_MAX padding), so every
 // list holds the same multiset as a member-by-member walk.
@@ -549,24 +639,40 @@ void old_mis(Ctx& c, int n, const int32_t* xadj, const int32_t* adj, OldMisOut& 
   FG_LAUNCH(scatter_bucket_kernel, grid_for(n, 256), 256, 0, s, n, fine.p, astart.p, cursor.p, members.p);
   segmented_sort_i32(members.p, astart.p, nagg, nullptr, s);
   // induced graph (getInducedGraph, misHelpers.cu:1078-1107): sorted unique neighbour aggregates
-  DBuf<int32_t> ccount(nagg + 1, s), coff(nagg + 1, s);
-  ccount.zero();
-  FG_LAUNCH(node_degree_to_agg_kernel, grid_for(n, 256), 256, 0, s, n, xadj, fine.p, ccount.p);
-  int64_t ncand = exclusive_scan(ccount.p, coff.p, nagg, s);
-  DBuf<int32_t> cand(ncand > 0 ? ncand : 1, s), ucount(nagg + 1, s), ixadj(nagg + 1, s);
+  DBuf<int32_t> ucount(nagg + 1, s), ixadj(nagg + 1, s), iadj;
+  DBuf<int32_t> mdeg(n + 1, s), noff(n + 1, s);
+  FG_LAUNCH(member_degree_kernel, grid_for(n, 256), 256, 0, s, n, members.p, xadj, mdeg.p);
+  exclusive_scan(mdeg.p, noff.p, n, s);
+  bool induced_done = false;
   {
-    DBuf<int32_t> mdeg(n + 1, s), noff(n + 1, s);
-    FG_LAUNCH(member_degree_kernel, grid_for(n, 256), 256, 0, s, n, members.p, xadj, mdeg.p);
-    exclusive_scan(mdeg.p, noff.p, n, s);
+    DBuf<int32_t> tmp((size_t)nagg * kIndCap, s), ovf(1, s);
+    ovf.zero();
+    FG_LAUNCH(induced_hash_kernel, (int)std::min<int64_t>((nagg + 7) / 8, 152 * 16), 256, 0, s, nagg, astart.p,
+              members.p, noff.p, xadj, adj, fine.p, tmp.p, ucount.p, ovf.p);
+    if (read_scalar(ovf.p, s) == 0) {
+      const int64_t innz = exclusive_scan(ucount.p, ixadj.p, nagg, s);
+      iadj.alloc(innz > 0 ? innz : 1, s);
+      FG_LAUNCH(compact_stride_kernel, grid_for((int64_t)nagg * 32, 256), 256, 0, s, nagg, tmp.p, kIndCap, ixadj.p,
+                iadj.p);
+      induced_done = true;
+    }
+  }
+  if (!induced_done) {
+    // an aggregate with more than kIndCap neighbour aggregates: sort every candidate list
+    DBuf<int32_t> ccount(nagg + 1, s), coff(nagg + 1, s);
+    ccount.zero();
+    FG_LAUNCH(node_degree_to_agg_kernel, grid_for(n, 256), 256, 0, s, n, xadj, fine.p, ccount.p);
+    int64_t ncand = exclusive_scan(ccount.p, coff.p, nagg, s);
+    DBuf<int32_t> cand(ncand > 0 ? ncand : 1, s);
     FG_LAUNCH(induced_candidates_nodes_kernel, grid_for(n, 256), 256, 0, s, n, members.p, noff.p, xadj, adj, fine.p,
               cand.p);
+    segmented_sort_i32(cand.p, coff.p, nagg, ucount.p, s);
+    FG_LAUNCH(drop_padding_kernel, grid_for(nagg, 256), 256, 0, s, nagg, coff.p, ucount.p, cand.p);
+    int64_t innz = exclusive_scan(ucount.p, ixadj.p, nagg, s);
+    iadj.alloc(innz > 0 ? innz : 1, s);
+    FG_LAUNCH(compact_segments_kernel, grid_for((int64_t)nagg * 32, 256), 256, 0, s, nagg, cand.p, coff.p, ixadj.p,
+              iadj.p);
   }
-  segmented_sort_i32(cand.p, coff.p, nagg, ucount.p, s);
-  FG_LAUNCH(drop_padding_kernel, grid_for(nagg, 256), 256, 0, s, nagg, coff.p, ucount.p, cand.p);
-  int64_t innz = exclusive_scan(ucount.p, ixadj.p, nagg, s);
-  DBuf<int32_t> iadj(innz > 0 ? innz : 1, s);
-  FG_LAUNCH(compact_segments_kernel, grid_for((int64_t)nagg * 32, 256), 256, 0, s, nagg, cand.p, coff.p, ixadj.p,
-            iadj.p);
   pt.mark("induced");
   // partitions of aggregates (aggregateWeightedGraph, weights = aggregate sizes)
   DBuf<int32_t> coarse;
