@@ -1431,12 +1431,26 @@ __global__ void __launch_bounds__(kRowThreads) spgemm_row_kernel(EscArgs<T> a, c
   if (i >= a.n) return;
   int u = 0;
   bool overflow = false;
-  for (int e = a.arp[i]; e < a.arp[i + 1] && !overflow; e++) {
-    const int k = a.aci[e];
-    const T av = a.av[e];
-    for (int f = a.brp[k]; f < a.brp[k + 1]; f++) {
+  const int ea = a.arp[i], eb = a.arp[i + 1];
+  for (int e0 = ea; e0 < eb && !overflow; e0 += 8) {
+    // 8 left entries at a time: their columns, values and right-row ranges are loaded
+    // before the products (which then run in generation order)
+    int kk[8], fb[8], fe[8];
+    T avv[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      kk[q] = e0 + q < eb ? a.aci[e0 + q] : 0;
+      avv[q] = e0 + q < eb ? a.av[e0 + q] : (T)0;
+    }
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      fb[q] = e0 + q < eb ? a.brp[kk[q]] : 0;
+      fe[q] = e0 + q < eb ? a.brp[kk[q] + 1] : 0;
+    }
+    for (int m = 0; m < 8 && !overflow; m++)
+    for (int f = fb[m]; f < fe[m]; f++) {
       const int j = a.bci[f];
-      const T p = av * a.bv[f];
+      const T p = avv[m] * a.bv[f];
       int q = 0;
       while (q < u && sc[q][t] != j) q++;
       if (q < u) {
