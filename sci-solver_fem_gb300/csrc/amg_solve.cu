@@ -864,6 +864,82 @@ __global__ void slice_entries_kernel(int ngroups, int C, const int32_t* grows, c
   out[i] = irp[rs + se] - irp[rs + ss];
 }
 
+// Cross-partition products with S lanes per row, for levels with long rows: lane j
+// forms the products of entries j, j + S, ... (4 rounds of loads in flight), and lane 0
+// of the row receives them through shuffles and adds them in entry order -- the same
+// sums as the per-thread gathers.
+// RHS == false: out_i = base_i - (sum of the row's products, from 0)   (the residual);
+// RHS == true:  out_i = base_i - p_0 - p_1 - ...                        (b' = b - A_out x).
+template <class T, bool RHS, int S>
+__global__ void aout_lanes_kernel(int n, const int32_t* __restrict__ orp, const int32_t* __restrict__ oci,
+                                  const T* __restrict__ ov, const T* base, const T* __restrict__ x, T* out) {
+  const int g = (blockIdx.x * blockDim.x + threadIdx.x) / S, j = threadIdx.x & (S - 1);
+  const bool live = g < n;
+  int a = 0, b = 0;
+  if (live) {
+    a = orp[g];
+    b = orp[g + 1];
+  }
+  T acc = live ? base[g] : (T)0, sum = (T)0;
+  const int rounds = (b - a + S - 1) / S;
+  const int wmax = __reduce_max_sync(0xffffffffu, rounds);  // warp-uniform trip count
+  for (int m0 = 0; m0 < wmax; m0 += 4) {
+    int c[4];
+    T v[4], p[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int q = a + (m0 + k) * S + j;
+      c[k] = q < b ? oci[q] : 0;
+      v[k] = q < b ? ov[q] : (T)0;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int q = a + (m0 + k) * S + j;
+      p[k] = q < b ? v[k] * x[c[k]] : (T)0;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+#pragma unroll
+      for (int t = 0; t < S; t++) {
+        const T pt = __shfl_sync(0xffffffffu, p[k], t, S);
+        if (j == 0 && a + (m0 + k) * S + t < b) {
+          if (RHS) acc = acc - pt;
+          else sum = sum + pt;
+        }
+      }
+  }
+  if (live && j == 0) out[g] = RHS ? acc : acc - sum;
+}
+
+// Lanes per row of the cross-partition kernels: 1 (per-thread gather) below 8 entries
+// per row on average, else a power of two near a quarter of the average row.
+template <class T>
+int aout_lanes(const Level<T>& L) {
+  const double avg = L.n > 0 ? (double)L.Aout.nnz / L.n : 0.0;
+  if (avg < 8.0) return 1;
+  int s = 2;
+  while (s < 32 && s * 4 < avg) s <<= 1;
+  return s;
+}
+
+template <class T, bool RHS>
+void launch_aout_lanes(cudaStream_t st, const Level<T>& L, int S, const T* base, const T* x, T* out) {
+  const int g = grid_for((int64_t)L.n * S, 256);
+#define FG_AOUT(SS)                                                                                   \
+  FG_LAUNCH((aout_lanes_kernel<T, RHS, SS>), g, 256, 0, st, L.n, L.Aout.rp.p, L.Aout.ci.p, L.Aout.v.p, base, x, out)
+  switch (S) {
+    case 2: FG_AOUT(2); break;
+    case 4: FG_AOUT(4); break;
+    case 8: FG_AOUT(8); break;
+    case 16: FG_AOUT(16); break;
+    default: FG_AOUT(32); break;
+  }
+#undef FG_AOUT
+}
+
+template <class T>
+void aout_rhs(cudaStream_t s, const Level<T>& L, const T* b, const T* x, T* bp);
+
 // Post-smoother right-hand side b' = b - A_out x (the first loop of
 // postRelaxSym_kernel, gauss_seidel.cu:3676-3684), one thread per row.
 template <class T>
@@ -874,6 +950,27 @@ __global__ void aout_rhs_kernel(int n, const int32_t* __restrict__ orp, const in
   if (i >= n) return;
   // acc + (-v) x and acc - v x round identically: the negation is exact
   bp[i] = gather_row<T, 8, true>(oci, ov, x, orp[i], orp[i + 1], 1, b[i]);
+}
+
+template <class T>
+void aout_rhs(cudaStream_t s, const Level<T>& L, const T* b, const T* x, T* bp) {
+  const int S = aout_lanes(L);
+  if (S > 1)
+    launch_aout_lanes<T, true>(s, L, S, b, x, bp);
+  else
+    FG_LAUNCH(aout_rhs_kernel<T>, grid_for(L.n, 256), 256, 0, s, L.n, L.Aout.rp.p, L.Aout.ci.p, L.Aout.v.p, b, x,
+              bp);
+}
+
+// r -= A_out x (preAout_kernel, gauss_seidel.cu:1977-2015).
+template <class T>
+void aout_residual(cudaStream_t s, const Level<T>& L, const T* x, T* r) {
+  const int S = aout_lanes(L);
+  if (S > 1)
+    launch_aout_lanes<T, false>(s, L, S, r, x, r);
+  else
+    FG_LAUNCH(aout_residual_kernel<T>, grid_for(L.n, 256), 256, 0, s, L.n, L.Aout.rp.p, L.Aout.ci.p, L.Aout.v.p, x,
+              r);
 }
 
 // The partition-block sweeps alone; a post relax reads its right-hand side b' =
@@ -918,8 +1015,7 @@ void smooth_sweeps(Ctx& c, Level<T>& L, bool post, const T* b, const T* xin, T* 
 template <class T>
 void smooth(Ctx& c, Level<T>& L, bool post, const T* b, const T* xin, T* xout, T* rout) {
   if (post) {
-    FG_LAUNCH(aout_rhs_kernel<T>, grid_for(L.n, 256), 256, 0, c.stream, L.n, L.Aout.rp.p, L.Aout.ci.p, L.Aout.v.p, b,
-              xin, L.bp.p);
+    aout_rhs<T>(c.stream, L, b, xin, L.bp.p);
     b = L.bp.p;
   }
   smooth_sweeps<T>(c, L, post, b, xin, xout, rout);
@@ -954,8 +1050,7 @@ void vcycle(Ctx& c, Hierarchy<T>& H, int l, const T* b_in, T* x_out, double* z_o
   }
   smooth<T>(c, L, false, b, nullptr, L.x.p, L.r.p);
   stage_mark(c, "pre", l);
-  FG_LAUNCH(aout_residual_kernel<T>, grid_for(n, 256), 256, 0, s, n, L.Aout.rp.p, L.Aout.ci.p, L.Aout.v.p, L.x.p,
-            L.r.p);
+  aout_residual<T>(s, L, L.x.p, L.r.p);
   stage_mark(c, "residual", l);
   // next level: input in its t (or b when coarsest), output in its xo (or x)
   Level<T>& N = *H.L[l + 1];
@@ -1394,8 +1489,7 @@ void profile_level0(Ctx& c, Hierarchy<T>& H, int which, int reps, double* ms, do
     }
   };
   if (which == 2)  // the post relax's right-hand side, computed once outside the timing
-    FG_LAUNCH(aout_rhs_kernel<T>, grid_for(n, 256), 256, 0, s, n, L.Aout.rp.p, L.Aout.ci.p, L.Aout.v.p, L.b.p, L.x.p,
-              L.bp.p);
+    aout_rhs<T>(s, L, L.b.p, L.x.p, L.bp.p);
   // in-partition entries: value + 16-bit column on the register path, + 32-bit column otherwise
   const double ein = smoother_in_registers(L.max_in_row, L.max_part_rows) ? ts + 2 : ts + 4;
   switch (which) {
