@@ -2174,6 +2174,43 @@ __global__ void permuted_values_kernel(int n, const int32_t* __restrict__ prp, c
   }
 }
 
+// Entries of each 32-row slice (32 x its longest row), for the sliced layout of the
+// permuted FP64 operator.
+__global__ void slice_width_kernel(int n, int nslices, const int32_t* __restrict__ prp, int32_t* __restrict__ cnt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if ((i >> 5) >= nslices) return;  // whole warps: nslices * 32 threads are live
+  const int len = i < n ? prp[i + 1] - prp[i] : 0;
+  const int w = __reduce_max_sync(0xffffffffu, len);
+  if ((i & 31) == 0) cnt[i >> 5] = 32 * w;
+}
+
+// The permuted operator written as slices: row i's entry k (in the sorted pattern's
+// order) goes to off[i / 32] + 32 k + i % 32, its value looked up in A as in
+// permuted_values_kernel; the slice's remaining slots get column -1 and value 0.
+__global__ void sliced_values_kernel(int n, int nslices, const int32_t* __restrict__ prp,
+                                     const int32_t* __restrict__ pci, const int32_t* __restrict__ iperm,
+                                     const int32_t* __restrict__ arp, const int32_t* __restrict__ aci,
+                                     const double* __restrict__ av, const int32_t* __restrict__ off,
+                                     int32_t* __restrict__ sci, double* __restrict__ sv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int sl = i >> 5;
+  if (sl >= nslices) return;
+  const int base = off[sl] + (i & 31), w = (off[sl + 1] - off[sl]) >> 5;
+  int k = 0;
+  if (i < n) {
+    const int r = iperm[i], a0 = arp[r], a1 = arp[r + 1], e0 = prp[i], e1 = prp[i + 1];
+    for (; k < e1 - e0; k++) {
+      const int col = pci[e0 + k];
+      sci[base + 32 * k] = col;
+      sv[base + 32 * k] = av[lower_bound_i32(aci, a0, a1, iperm[col])];
+    }
+  }
+  for (; k < w; k++) {
+    sci[base + 32 * k] = -1;
+    sv[base + 32 * k] = 0.0;
+  }
+}
+
 void amg_setup(Ctx& c) {
   cudaStream_t s = c.stream;
   FG_REQUIRE(c.has_matrix, FEMGPU_ERR_NOT_READY, "no operator: call femgpu_set_mesh + femgpu_assemble or femgpu_set_matrix_csr");
@@ -2223,13 +2260,40 @@ void amg_setup(Ctx& c) {
     c.A0p.n = c.A0p.m = n;
     c.A0p.nnz = pnnz;
     c.A0p.rp.alloc(n + 1, s);
-    c.A0p.ci.alloc(pnnz > 0 ? pnnz : 1, s);
-    c.A0p.v.alloc(pnnz > 0 ? pnnz : 1, s);
     FG_CUDA(cudaMemcpyAsync(c.A0p.rp.p, prp, (n + 1) * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
-    if (pnnz > 0)
-      FG_CUDA(cudaMemcpyAsync(c.A0p.ci.p, pci, pnnz * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
-    FG_LAUNCH(permuted_values_kernel, grid_for(n, 128), 128, 0, s, n, c.A0p.rp.p, c.A0p.ci.p, iperm.p, c.A.rp.p,
-              c.A.ci.p, c.A.v.p, c.A0p.v.p);
+    // Slices of 32 rows when they pad the operator by at most 1/8 (mesh operators,
+    // whose neighbouring rows have similar lengths); otherwise CSR.
+    const int nslices = (n + 31) / 32;
+    c.sliced = false;
+    c.s_off.release();
+    c.s_ci.release();
+    c.s_v.release();
+    c.A0p.ci.release();
+    c.A0p.v.release();
+    if (n > 0) {
+      c.s_off.alloc(nslices + 1, s);
+      FG_LAUNCH(slice_width_kernel, grid_for((int64_t)nslices * 32, 256), 256, 0, s, n, nslices, c.A0p.rp.p,
+                c.s_off.p);
+      const int64_t padded = exclusive_scan(c.s_off.p, c.s_off.p, nslices, s);
+      if (padded <= INT32_MAX && padded <= pnnz + pnnz / 8) {
+        c.sliced = true;
+        c.s_padded = padded;
+        c.s_ci.alloc(padded > 0 ? padded : 1, s);
+        c.s_v.alloc(padded > 0 ? padded : 1, s);
+        FG_LAUNCH(sliced_values_kernel, grid_for((int64_t)nslices * 32, 128), 128, 0, s, n, nslices, c.A0p.rp.p,
+                  pci, iperm.p, c.A.rp.p, c.A.ci.p, c.A.v.p, c.s_off.p, c.s_ci.p, c.s_v.p);
+      } else {
+        c.s_off.release();
+      }
+    }
+    if (!c.sliced) {
+      c.A0p.ci.alloc(pnnz > 0 ? pnnz : 1, s);
+      c.A0p.v.alloc(pnnz > 0 ? pnnz : 1, s);
+      if (pnnz > 0)
+        FG_CUDA(cudaMemcpyAsync(c.A0p.ci.p, pci, pnnz * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
+      FG_LAUNCH(permuted_values_kernel, grid_for(n, 128), 128, 0, s, n, c.A0p.rp.p, c.A0p.ci.p, iperm.p, c.A.rp.p,
+                c.A.ci.p, c.A.v.p, c.A0p.v.p);
+    }
   }
   FG_CUDA(cudaEventRecord(e1, s));
   FG_CUDA(cudaEventSynchronize(e1));

@@ -704,6 +704,62 @@ __global__ void spmv_dot_kernel(int n, const int32_t* __restrict__ rp, const int
   }
 }
 
+// Row i of the sliced operator: its entries in order (padding, column -1, comes after
+// them and is skipped), in groups of 8 loads in flight; the same fused multiply-adds
+// as the CSR loop.  The 32 rows of a slice are the 32 lanes of a warp, so each load
+// instruction reads 32 consecutive columns or values.
+__device__ __forceinline__ double sliced_row(int i, const int32_t* __restrict__ off, const int32_t* __restrict__ ci,
+                                             const double* __restrict__ v, const double* __restrict__ p) {
+  const int sl = i >> 5, e1 = off[sl + 1];
+  double s = 0.0;
+  for (int e0 = off[sl] + (i & 31); e0 < e1; e0 += 256) {
+    int c[8];
+    double w[8], x[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      const int q = e0 + 32 * k;
+      c[k] = q < e1 ? ci[q] : -1;
+      w[k] = q < e1 ? v[q] : 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < 8; k++) x[k] = c[k] >= 0 ? p[c[k]] : 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+      if (c[k] >= 0) s = fma(w[k], x[k], s);
+  }
+  return s;
+}
+
+// spmv_dot_kernel on the sliced operator: the same rows per thread (the grid is a
+// whole number of warps, so a warp's 32 rows are one slice) and the same sums.
+__global__ void spmv_dot_sliced_kernel(int n, const int32_t* __restrict__ off, const int32_t* __restrict__ ci,
+                                       const double* __restrict__ v, const double* __restrict__ p,
+                                       double* __restrict__ y, double* __restrict__ partial, double* sc,
+                                       unsigned* counter) {
+  __shared__ double sh[32];
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double s = sliced_row(i, off, ci, v, p);
+    y[i] = s;
+    acc = fma(s, p[i], acc);
+  }
+  double t = block_sum(acc, sh);
+  if (threadIdx.x == 0) partial[blockIdx.x] = t;
+  if (!last_block_done(counter)) return;
+  const double yp = ordered_total(partial, gridDim.x, sh);
+  if (threadIdx.x == 0) {
+    sc[S_YP] = yp;
+    alpha_update(sc);
+    *counter = 0u;
+  }
+}
+
+__global__ void spmv_sliced_kernel(int n, const int32_t* __restrict__ off, const int32_t* __restrict__ ci,
+                                   const double* __restrict__ v, const double* __restrict__ x, double* __restrict__ y) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = sliced_row(i, off, ci, v, x);
+}
+
 // z.r (and z.r_old for the flexible beta) with the totals and beta formed by the
 // last block (same sums as dot_kernel + finalize_kernel + the beta step).
 __global__ void dot_beta_kernel(int n, const double* __restrict__ z, const double* __restrict__ r,
@@ -1292,8 +1348,21 @@ namespace {
 // y = A0p p with p.y and alpha.
 void launch_spmv_dot(Ctx& c, int n, const double* p, double* y) {
   const DCsr<double>& A = c.A0p;
-  FG_LAUNCH(spmv_dot_kernel, kRedBlocks, kRedThreads, 0, c.stream, n, A.rp.p, A.ci.p, A.v.p, p, y, c.red.p,
-            c.red.p + 2 * kRedBlocks, c.rcount.p + 1);
+  if (c.sliced)
+    FG_LAUNCH(spmv_dot_sliced_kernel, kRedBlocks, kRedThreads, 0, c.stream, n, c.s_off.p, c.s_ci.p, c.s_v.p, p, y,
+              c.red.p, c.red.p + 2 * kRedBlocks, c.rcount.p + 1);
+  else
+    FG_LAUNCH(spmv_dot_kernel, kRedBlocks, kRedThreads, 0, c.stream, n, A.rp.p, A.ci.p, A.v.p, p, y, c.red.p,
+              c.red.p + 2 * kRedBlocks, c.rcount.p + 1);
+}
+
+// y = A0p x.
+void launch_spmv_a0(Ctx& c, int n, const double* x, double* y) {
+  const DCsr<double>& A = c.A0p;
+  if (c.sliced)
+    FG_LAUNCH(spmv_sliced_kernel, grid_for(n, 256), 256, 0, c.stream, n, c.s_off.p, c.s_ci.p, c.s_v.p, x, y);
+  else
+    FG_LAUNCH(spmv_kernel, grid_for(n, 256), 256, 0, c.stream, n, A.rp.p, A.ci.p, A.v.p, x, y);
 }
 
 void pcg_iteration_body(Ctx& c, int n, int flexible, bool to_host) {
@@ -1302,7 +1371,6 @@ void pcg_iteration_body(Ctx& c, int n, int flexible, bool to_host) {
   double* part2 = c.red.p + kRedBlocks;
   double* sc = c.red.p + 2 * kRedBlocks;
   unsigned* cnt = c.rcount.p;
-  const DCsr<double>& A = c.A0p;
   precondition_any(c, c.vr.p, c.vz.p);
   FG_LAUNCH(dot_beta_kernel, kRedBlocks, kRedThreads, 0, s, n, c.vz.p, c.vr.p, flexible ? c.vrold.p : nullptr, part,
             part2, sc, flexible, cnt);
@@ -1379,14 +1447,13 @@ SolveResult amg_solve_device(Ctx& c, const double* d_b, double* d_x) {
   SolveResult res;
   double* part = c.red.p;
   double* sc = c.red.p + 2 * kRedBlocks;
-  const DCsr<double>& A = c.A0p;
   FG_LAUNCH(perm_vec_in_kernel, grid_for(n, 256), 256, 0, s, n, c.perm0.p, d_b, c.vb.p);
   FG_LAUNCH(perm_vec_in_kernel, grid_for(n, 256), 256, 0, s, n, c.perm0.p, d_x, c.vx.p);
   if (c.cfg.solverType == 0) {
     // AMG_SOLVER: one V-cycle applied to b (amg.cu:150-160); x is overwritten
     precondition_any(c, c.vb.p, c.vx.p);
     FG_LAUNCH(perm_vec_out_kernel, grid_for(n, 256), 256, 0, s, n, c.perm0.p, c.vx.p, d_x);
-    FG_LAUNCH(spmv_kernel, grid_for(n, 256), 256, 0, s, n, A.rp.p, A.ci.p, A.v.p, c.vx.p, c.vy.p);
+    launch_spmv_a0(c, n, c.vx.p, c.vy.p);
     FG_LAUNCH(residual_kernel, kRedBlocks, kRedThreads, 0, s, n, c.vb.p, c.vy.p, c.vr.p, part);
     FG_LAUNCH(finalize_kernel, 1, 1024, 0, s, part, kRedBlocks, sc + S_NR);
     FG_LAUNCH(dot_kernel, kRedBlocks, kRedThreads, 0, s, n, c.vb.p, c.vb.p, nullptr, part, nullptr);
@@ -1401,7 +1468,7 @@ SolveResult amg_solve_device(Ctx& c, const double* d_b, double* d_x) {
   const int flexible = c.cfg.flexibleCG;
   FG_LAUNCH(dot_kernel, kRedBlocks, kRedThreads, 0, s, n, c.vb.p, c.vb.p, nullptr, part, nullptr);
   FG_LAUNCH(finalize_kernel, 1, 1024, 0, s, part, kRedBlocks, sc + S_BN);
-  FG_LAUNCH(spmv_kernel, grid_for(n, 256), 256, 0, s, n, A.rp.p, A.ci.p, A.v.p, c.vx.p, c.vy.p);
+  launch_spmv_a0(c, n, c.vx.p, c.vy.p);
   FG_LAUNCH(residual_kernel, kRedBlocks, kRedThreads, 0, s, n, c.vb.p, c.vy.p, c.vr.p, part);
   FG_LAUNCH(finalize_kernel, 1, 1024, 0, s, part, kRedBlocks, sc + S_NR);
   FG_LAUNCH(set_slot_kernel, 1, 1, 0, s, sc, S_FLAG, 0.0);
@@ -1552,7 +1619,9 @@ void profile_kernel(Ctx& c, int which, int reps, double* ms, double* bytes) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     *ms = t / reps;
-    *bytes = 12.0 * c.A0p.nnz + 4.0 * (n + 1) + 8.0 * n + 8.0 * n;
+    // entries (value + column), row (or slice) offsets, p read and y written
+    *bytes = c.sliced ? 12.0 * c.A0p.nnz + 4.0 * ((n + 31) / 32 + 1) + 16.0 * n
+                      : 12.0 * c.A0p.nnz + 4.0 * (n + 1) + 16.0 * n;
     return;
   }
   if (c.cfg.precision == 1) profile_level0(c, static_cast<Hierarchy<double>&>(*c.H), which, reps, ms, bytes);

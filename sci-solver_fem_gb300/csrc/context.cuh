@@ -126,6 +126,12 @@ struct Ctx {
   std::unique_ptr<HierarchyBase> H;
   DBuf<int32_t> perm0;           // level-0 old -> new (identity if level 0 is the coarsest)
   DCsr<double> A0p;              // FP64 level-0 operator in permuted order (outer PCG)
+  // The same operator as slices of 32 rows (used instead of A0p when padding is small):
+  // entry k of row 32 s + j sits at s_off[s] + 32 k + j; padding has column -1.
+  bool sliced = false;
+  int64_t s_padded = 0;
+  DBuf<int32_t> s_off, s_ci;
+  DBuf<double> s_v;
   bool has_hierarchy = false;
   double setup_ms = 0.0;
 
