@@ -313,6 +313,29 @@ __global__ void __launch_bounds__(1024) smooth_creg_kernel(
   }
 }
 
+// Row sum s +/- v[q] x[ci[q]] over q = e, e + stride, ... < end, added in that order
+// with separately rounded products; the first K entries' columns, values and x are
+// all loaded before the first add, so a short row costs three dependent loads.
+template <class T, int K, bool SUB>
+__device__ __forceinline__ T gather_row(const int32_t* __restrict__ ci, const T* __restrict__ v,
+                                        const T* __restrict__ x, int e, int end, int stride, T s) {
+  int c[K];
+  T a[K], xv[K];
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    const int q = e + k * stride;
+    c[k] = q < end ? ci[q] : 0;
+    a[k] = q < end ? v[q] : (T)0;
+  }
+#pragma unroll
+  for (int k = 0; k < K; k++) xv[k] = e + k * stride < end ? x[c[k]] : (T)0;
+#pragma unroll
+  for (int k = 0; k < K; k++)
+    if (e + k * stride < end) s = SUB ? s - a[k] * xv[k] : s + a[k] * xv[k];
+  for (int q = e + K * stride; q < end; q += stride) s = SUB ? s - v[q] * x[ci[q]] : s + v[q] * x[ci[q]];
+  return s;
+}
+
 // Shared memory of the register smoother: two mbarriers, x twice (kRegGroupRows + 1
 // slots each; the last slot stays 0 for padded entries), then two staging buffers for
 // a group's in-partition values and 16-bit local columns (ecap entries each, filled
@@ -365,12 +388,20 @@ __device__ __forceinline__ void stage_group(unsigned char* sm, const RegSmemLayo
 // sweeps; x is double-buffered in shared memory (one barrier per sweep).  Row sums
 // are the one-lane case of the shared-memory smoother: fused multiply-adds in entry
 // order.  A copy that does not land within the wait limit sets *kerr and ends the CTA.
+// Level-0 fusions (each off when its pointer is null):
+// - pre relax, b64: the right-hand side is read in FP64 and rounded to T here (and
+//   stored to b_store for the post relax) instead of by a separate cast;
+// - post relax, orp/oci/ov: b' = b - A_out x_in is formed here, with the same
+//   subtractions in the same order as aout_rhs_kernel;
+// - z64: x is written widened to FP64 there instead of to x_out.
 template <class T, bool POST, int K>
 __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
     int ngroups, const int32_t* __restrict__ grows, const int32_t* __restrict__ irp,
     const uint16_t* __restrict__ c16, const T* __restrict__ iv, const T* __restrict__ diag,
     const T* __restrict__ dinv, const T* __restrict__ b, T w, int inner, const T* __restrict__ x_in,
-    T* __restrict__ x_out, T* __restrict__ r_out, int ecap, double* __restrict__ kerr) {
+    T* __restrict__ x_out, T* __restrict__ r_out, int ecap, double* __restrict__ kerr,
+    const double* __restrict__ b64, T* __restrict__ b_store, const int32_t* __restrict__ orp,
+    const int32_t* __restrict__ oci, const T* __restrict__ ov, double* __restrict__ z64) {
   extern __shared__ __align__(128) unsigned char sm[];
   const RegSmemLayout Ls = reg_smem_layout<T>(ecap);
   uint64_t* bar = reinterpret_cast<uint64_t*>(sm);
@@ -404,8 +435,19 @@ __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
       len = irp[row + 1] - e0;
       d = diag[row];
       di = dinv[row];
-      bb = b[row];
-      x = POST ? x_in[row] : (w * bb) * di;
+      if (POST) {
+        bb = b[row];
+        if (orp) bb = gather_row<T, 8, true>(oci, ov, x_in, orp[row], orp[row + 1], 1, bb);
+        x = x_in[row];
+      } else {
+        if (b64) {
+          bb = (T)b64[row];
+          b_store[row] = bb;
+        } else {
+          bb = b[row];
+        }
+        x = (w * bb) * di;
+      }
       xa[t] = x;
     }
     const bool ok = mbar_wait_bounded(bar + buf, parity);
@@ -452,7 +494,8 @@ __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
       last = xb;
     }
     if (live) {
-      x_out[row] = x;
+      if (z64) z64[row] = (double)x;
+      else x_out[row] = x;
       if (!POST) {
         T sax = 0;
 #pragma unroll
@@ -466,29 +509,6 @@ __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
 }
 
 // r -= A_out x (preAout_kernel, gauss_seidel.cu:1977-2015).
-// Row sum s +/- v[q] x[ci[q]] over q = e, e + stride, ... < end, added in that order
-// with separately rounded products; the first K entries' columns, values and x are
-// all loaded before the first add, so a short row costs three dependent loads.
-template <class T, int K, bool SUB>
-__device__ __forceinline__ T gather_row(const int32_t* __restrict__ ci, const T* __restrict__ v,
-                                        const T* __restrict__ x, int e, int end, int stride, T s) {
-  int c[K];
-  T a[K], xv[K];
-#pragma unroll
-  for (int k = 0; k < K; k++) {
-    const int q = e + k * stride;
-    c[k] = q < end ? ci[q] : 0;
-    a[k] = q < end ? v[q] : (T)0;
-  }
-#pragma unroll
-  for (int k = 0; k < K; k++) xv[k] = e + k * stride < end ? x[c[k]] : (T)0;
-#pragma unroll
-  for (int k = 0; k < K; k++)
-    if (e + k * stride < end) s = SUB ? s - a[k] * xv[k] : s + a[k] * xv[k];
-  for (int q = e + K * stride; q < end; q += stride) s = SUB ? s - v[q] * x[ci[q]] : s + v[q] * x[ci[q]];
-  return s;
-}
-
 template <class T>
 __global__ void aout_residual_kernel(int n, const int32_t* __restrict__ orp, const int32_t* __restrict__ oci,
                                      const T* __restrict__ ov, const T* __restrict__ x, T* __restrict__ r) {
@@ -1029,10 +1049,20 @@ void aout_residual(cudaStream_t s, const Level<T>& L, const T* x, T* r) {
               r);
 }
 
-// The partition-block sweeps alone; a post relax reads its right-hand side b' =
-// b - A_out x_in from b (as computed by aout_rhs_kernel).
+// Fused level-0 inputs and outputs of the register smoother (all null: none).
 template <class T>
-void smooth_sweeps(Ctx& c, Level<T>& L, bool post, const T* b, const T* xin, T* xout, T* rout) {
+struct RegFusion {
+  const double* b64 = nullptr;  // pre relax: FP64 right-hand side, rounded to T in the kernel ...
+  T* b_store = nullptr;         // ... and stored here
+  bool aout = false;            // post relax: b' = b - A_out x_in formed in the kernel
+  double* z64 = nullptr;        // result widened to FP64 here instead of xout
+};
+
+// The partition-block sweeps alone; a post relax reads its right-hand side b' =
+// b - A_out x_in from b (as computed by aout_rhs_kernel) unless f.aout.
+template <class T>
+void smooth_sweeps(Ctx& c, Level<T>& L, bool post, const T* b, const T* xin, T* xout, T* rout,
+                   const RegFusion<T>& f = RegFusion<T>()) {
   cudaStream_t s = c.stream;
   const int32_t* aorp = post ? nullptr : L.Aout.rp.p;
   const T w = (T)c.cfg.smootherWeight;
@@ -1043,7 +1073,8 @@ void smooth_sweeps(Ctx& c, Level<T>& L, bool post, const T* b, const T* xin, T* 
       ensure_smem(k, L.smooth_smem);
     FG_LAUNCH(k, L.smooth_grid, L.smooth_threads, L.smooth_smem, s, L.ngroups, L.grows.p, L.Ain.rp.p, L.ci16.p,
               L.Ain.v.p, L.diag.p, L.dinv.p, b, w, inner, xin, xout, rout, L.max_group_ents + 16,
-              c.red.p + 2 * kRedBlocks + S_KERR);
+              c.red.p + 2 * kRedBlocks + S_KERR, f.b64, f.b_store, f.aout ? L.Aout.rp.p : nullptr,
+              f.aout ? L.Aout.ci.p : nullptr, f.aout ? L.Aout.v.p : nullptr, f.z64);
     return;
   }
   if (L.smooth_k > 0) {
@@ -1068,13 +1099,32 @@ void smooth_sweeps(Ctx& c, Level<T>& L, bool post, const T* b, const T* xin, T* 
 }
 
 // Pre relax (post == false) or post relax: b' = b - A_out x_in, then the sweeps.
+// b64 (pre relax): b is first rounded from this FP64 vector into b (b_store);
+// z64: the result goes to z64 in FP64 instead of xout.  The register smoother does
+// both (and b') inside its kernel; the other smoothers use separate kernels.
 template <class T>
-void smooth(Ctx& c, Level<T>& L, bool post, const T* b, const T* xin, T* xout, T* rout) {
+void smooth(Ctx& c, Level<T>& L, bool post, const T* b, const T* xin, T* xout, T* rout,
+            const double* b64 = nullptr, T* b_store = nullptr, double* z64 = nullptr) {
+  cudaStream_t s = c.stream;
+  if (smoother_in_registers(L.max_in_row, L.max_part_rows)) {
+    RegFusion<T> f;
+    f.b64 = post ? nullptr : b64;
+    f.b_store = post ? nullptr : b_store;
+    f.aout = post && L.Aout.nnz > 0;
+    f.z64 = z64;
+    smooth_sweeps<T>(c, L, post, b, xin, xout, rout, f);
+    return;
+  }
+  if (!post && b64) {
+    FG_LAUNCH(cast_in_kernel<T>, grid_for(L.n, 256), 256, 0, s, L.n, b64, b_store);
+    b = b_store;
+  }
   if (post) {
-    aout_rhs<T>(c.stream, L, b, xin, L.bp.p);
+    aout_rhs<T>(s, L, b, xin, L.bp.p);
     b = L.bp.p;
   }
   smooth_sweeps<T>(c, L, post, b, xin, xout, rout);
+  if (z64) FG_LAUNCH(cast_out_kernel<T>, grid_for(L.n, 256), 256, 0, s, L.n, xout, z64);
 }
 
 // Records a named event on the stream when stage timing is on (never during capture).
@@ -1087,9 +1137,12 @@ void stage_mark(Ctx& c, const char* what, int l) {
 }
 
 // b (level order for l > 0, already permuted for l == 0) -> x (same ordering).  At
-// level 0 with z_out != nullptr the result goes to z_out in FP64 instead of x_out.
+// level 0 with z_out != nullptr the result goes to z_out in FP64 instead of x_out;
+// with r64 != nullptr, b_in is first rounded from the FP64 vector r64 (by the
+// pre-smoother when it can, which also writes the rounded copy to b_in).
 template <class T>
-void vcycle(Ctx& c, Hierarchy<T>& H, int l, const T* b_in, T* x_out, double* z_out = nullptr) {
+void vcycle(Ctx& c, Hierarchy<T>& H, int l, T* b_in, T* x_out, double* z_out = nullptr,
+            const double* r64 = nullptr) {
   cudaStream_t s = c.stream;
   Level<T>& L = *H.L[l];
   const int n = L.A.n;
@@ -1104,7 +1157,7 @@ void vcycle(Ctx& c, Hierarchy<T>& H, int l, const T* b_in, T* x_out, double* z_o
     b = L.b.p;
     stage_mark(c, "permute_in", l);
   }
-  smooth<T>(c, L, false, b, nullptr, L.x.p, L.r.p);
+  smooth<T>(c, L, false, b, nullptr, L.x.p, L.r.p, r64, b_in);
   stage_mark(c, "pre", l);
   aout_residual<T>(s, L, L.x.p, L.r.p);
   stage_mark(c, "residual", l);
@@ -1117,15 +1170,19 @@ void vcycle(Ctx& c, Hierarchy<T>& H, int l, const T* b_in, T* x_out, double* z_o
   vcycle(c, H, l + 1, bc, xc);
   spmv_lanes(L.P, xc, L.x.p, 1, s);
   stage_mark(c, "prolong", l);
+  bool z_done = false;
   for (int rl = 0; rl < c.cfg.postRelaxes; rl++) {
-    smooth<T>(c, L, true, b, L.x.p, L.r.p, nullptr);
+    // the last post relax of level 0 writes z itself
+    double* z64 = (l == 0 && z_out && rl + 1 == c.cfg.postRelaxes) ? z_out : nullptr;
+    smooth<T>(c, L, true, b, L.x.p, L.r.p, nullptr, nullptr, nullptr, z64);
     std::swap(L.x.p, L.r.p);  // r is free after the restriction: use it as the ping-pong buffer
+    z_done = z64 != nullptr;
   }
   stage_mark(c, "post", l);
   if (l > 0) {
     FG_LAUNCH(permute_out_kernel<T>, grid_for(n, 256), 256, 0, s, n, L.iperm.p, L.x.p, x_out);
   } else if (z_out) {
-    FG_LAUNCH(cast_out_kernel<T>, grid_for(n, 256), 256, 0, s, n, L.x.p, z_out);
+    if (!z_done) FG_LAUNCH(cast_out_kernel<T>, grid_for(n, 256), 256, 0, s, n, L.x.p, z_out);
   } else {
     FG_CUDA(cudaMemcpyAsync(x_out, L.x.p, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
   }
@@ -1140,13 +1197,12 @@ void precondition(Ctx& c, Hierarchy<T>& H, const double* r, double* z) {
   const int n = L.A.n;
   T* b = L.coarsest ? L.b.p : L.t.p;
   T* x = L.coarsest ? L.x.p : L.xo.p;
-  FG_LAUNCH(cast_in_kernel<T>, grid_for(n, 256), 256, 0, s, n, r, b);
-  stage_mark(c, "cast_in", 0);
   if (L.coarsest) {
+    FG_LAUNCH(cast_in_kernel<T>, grid_for(n, 256), 256, 0, s, n, r, b);
     vcycle(c, H, 0, b, x);
     FG_LAUNCH(cast_out_kernel<T>, grid_for(n, 256), 256, 0, s, n, x, z);
   } else {
-    vcycle(c, H, 0, b, x, z);  // level 0 writes z itself
+    vcycle(c, H, 0, b, x, z, r);  // level 0 reads r and writes z itself
   }
 }
 
