@@ -313,6 +313,11 @@ __global__ void __launch_bounds__(1024) smooth_creg_kernel(
   }
 }
 
+// PCG reduction helpers (defined with the PCG kernels below).
+__device__ double ordered_total(const double* partial, int nparts, double* sh);
+__device__ bool last_block_done(unsigned* counter);
+__device__ void beta_update(double* sc, int flexible);
+
 // Row sum s +/- v[q] x[ci[q]] over q = e, e + stride, ... < end, added in that order
 // with separately rounded products; the first K entries' columns, values and x are
 // all loaded before the first add, so a short row costs three dependent loads.
@@ -393,7 +398,11 @@ __device__ __forceinline__ void stage_group(unsigned char* sm, const RegSmemLayo
 //   stored to b_store for the post relax) instead of by a separate cast;
 // - post relax, orp/oci/ov: b' = b - A_out x_in is formed here, with the same
 //   subtractions in the same order as aout_rhs_kernel;
-// - z64: x is written widened to FP64 there instead of to x_out.
+// - z64: x is written widened to FP64 there instead of to x_out;
+// - dot_part (with z64): the CTA's partial sums of z.dot_r (and z.dot_o) go to
+//   dot_part[blockIdx.x] (and dot_part[gridDim.x + blockIdx.x]), each thread adding
+//   its rows in the order it smooths them, then block_sum; the CTA that finishes last
+//   (ticket dot_count) forms the ordered totals and the PCG beta in sc.
 template <class T, bool POST, int K>
 __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
     int ngroups, const int32_t* __restrict__ grows, const int32_t* __restrict__ irp,
@@ -401,8 +410,12 @@ __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
     const T* __restrict__ dinv, const T* __restrict__ b, T w, int inner, const T* __restrict__ x_in,
     T* __restrict__ x_out, T* __restrict__ r_out, int ecap, double* __restrict__ kerr,
     const double* __restrict__ b64, T* __restrict__ b_store, const int32_t* __restrict__ orp,
-    const int32_t* __restrict__ oci, const T* __restrict__ ov, double* __restrict__ z64) {
+    const int32_t* __restrict__ oci, const T* __restrict__ ov, double* __restrict__ z64,
+    const double* __restrict__ dot_r, const double* __restrict__ dot_o, double* __restrict__ dot_part,
+    unsigned* dot_count, double* sc, int flexible) {
   extern __shared__ __align__(128) unsigned char sm[];
+  __shared__ double sh_dot[32];
+  double dz1 = 0.0, dz2 = 0.0;
   const RegSmemLayout Ls = reg_smem_layout<T>(ecap);
   uint64_t* bar = reinterpret_cast<uint64_t*>(sm);
   T* const xa = reinterpret_cast<T*>(sm + Ls.x0);
@@ -430,11 +443,16 @@ __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
     const int row = rs + t;
     int e0 = 0, len = 0;
     T d = (T)1, di = (T)1, bb = (T)0, x = (T)0;
+    double dr = 0.0, dor = 0.0;  // the dot operands, loaded now so the sweeps hide their latency
     if (live) {
       e0 = irp[row];
       len = irp[row + 1] - e0;
       d = diag[row];
       di = dinv[row];
+      if (POST && dot_part) {
+        dr = dot_r[row];
+        if (dot_o) dor = dot_o[row];
+      }
       if (POST) {
         bb = b[row];
         if (orp) bb = gather_row<T, 8, true>(oci, ov, x_in, orp[row], orp[row + 1], 1, bb);
@@ -494,8 +512,16 @@ __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
       last = xb;
     }
     if (live) {
-      if (z64) z64[row] = (double)x;
-      else x_out[row] = x;
+      if (POST && z64) {
+        const double zr = (double)x;
+        z64[row] = zr;
+        if (dot_part) {
+          dz1 = fma(zr, dr, dz1);
+          if (dot_o) dz2 = fma(zr, dor, dz2);
+        }
+      } else {
+        x_out[row] = x;
+      }
       if (!POST) {
         T sax = 0;
 #pragma unroll
@@ -505,6 +531,23 @@ __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
       }
     }
     __syncthreads();  // x buffers and this staging buffer are free for the next group
+  }
+  if (POST && dot_part && z64) {
+    const double t1 = block_sum(dz1, sh_dot);
+    if (threadIdx.x == 0) dot_part[blockIdx.x] = t1;
+    if (dot_o) {
+      const double t2 = block_sum(dz2, sh_dot);
+      if (threadIdx.x == 0) dot_part[gridDim.x + blockIdx.x] = t2;
+    }
+    if (!last_block_done(dot_count)) return;
+    const double rzn = ordered_total(dot_part, gridDim.x, sh_dot);
+    const double zro = dot_o ? ordered_total(dot_part + gridDim.x, gridDim.x, sh_dot) : 0.0;
+    if (threadIdx.x == 0) {
+      sc[S_RZNEW] = rzn;
+      if (dot_o) sc[S_ZROLD] = zro;
+      beta_update(sc, flexible);
+      *dot_count = 0u;
+    }
   }
 }
 
@@ -585,12 +628,25 @@ __global__ void dot_kernel(int n, const double* __restrict__ a, const double* __
 // whose size divides 1024 gets the same bits (valid in thread 0).
 __device__ double ordered_total(const double* partial, int nparts, double* sh) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int vw = w; vw < 32; vw += nw) {
-    double v = 0.0;
-    for (int q = vw * 32 + lane; q < nparts; q += 1024) v += partial[q];
+  // a warp stands in for up to 4 virtual warps per pass; their first partials are
+  // loaded together (one L2 round trip) before the adds and butterflies
+  for (int vw0 = w; vw0 < 32; vw0 += 4 * nw) {
+    double v[4];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) sh[vw] = v;
+    for (int m = 0; m < 4; m++) {
+      const int q = (vw0 + m * nw) * 32 + lane;
+      v[m] = (vw0 + m * nw < 32 && q < nparts) ? 0.0 + partial[q] : 0.0;  // 0 + x: the sum's first add
+    }
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+      const int vw = vw0 + m * nw;
+      if (vw < 32) {
+        for (int q = vw * 32 + lane + 1024; q < nparts; q += 1024) v[m] += partial[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[m] += __shfl_xor_sync(0xffffffffu, v[m], o);
+        if (lane == 0) sh[vw] = v[m];
+      }
+    }
   }
   __syncthreads();
   double t = 0.0;
@@ -644,7 +700,28 @@ __global__ void update_kernel(int n, double* __restrict__ sc, const double* __re
   __shared__ double sh[32];
   const double alpha = sc[S_ALPHA];
   double acc = 0.0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  // elements i, i + G, i + 2G, ... in order; four at a time with all loads issued first
+  const int G = gridDim.x * blockDim.x;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + 3 * G < n; i += 4 * G) {
+    double rr[4], pp[4], xx[4], yy[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      rr[u] = r[i + u * G];
+      pp[u] = p[i + u * G];
+      xx[u] = x[i + u * G];
+      yy[u] = y[i + u * G];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      if (rold) rold[i + u * G] = rr[u];
+      x[i + u * G] = fma(alpha, pp[u], xx[u]);
+      const double ri = fma(-alpha, yy[u], rr[u]);
+      r[i + u * G] = ri;
+      acc = fma(ri, ri, acc);
+    }
+  }
+  for (; i < n; i += G) {
     double ri = r[i];
     if (rold) rold[i] = ri;
     x[i] = fma(alpha, p[i], x[i]);
@@ -787,7 +864,24 @@ __global__ void dot_beta_kernel(int n, const double* __restrict__ z, const doubl
                                 int flexible, unsigned* counter) {
   __shared__ double sh[32];
   double s1 = 0.0, s2 = 0.0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  // elements i, i + G, ... in order; four at a time with all loads issued first
+  const int G = gridDim.x * blockDim.x;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + 3 * G < n; i += 4 * G) {
+    double zz[4], rr[4], oo[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      zz[u] = z[i + u * G];
+      rr[u] = r[i + u * G];
+      oo[u] = rold ? rold[i + u * G] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      s1 = fma(zz[u], rr[u], s1);
+      if (rold) s2 = fma(zz[u], oo[u], s2);
+    }
+  }
+  for (; i < n; i += G) {
     s1 = fma(z[i], r[i], s1);
     if (rold) s2 = fma(z[i], rold[i], s2);
   }
@@ -825,7 +919,19 @@ __global__ void set_slot_kernel(double* sc, int slot, double v) { sc[slot] = v; 
 __global__ void pupdate_kernel(int n, const double* __restrict__ sc, const double* __restrict__ z,
                                double* __restrict__ p) {
   const double beta = sc[S_BETA];
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = fma(beta, p[i], z[i]);
+  const int G = gridDim.x * blockDim.x;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + 3 * G < n; i += 4 * G) {
+    double pp[4], zz[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      pp[u] = p[i + u * G];
+      zz[u] = z[i + u * G];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) p[i + u * G] = fma(beta, pp[u], zz[u]);
+  }
+  for (; i < n; i += G) p[i] = fma(beta, p[i], z[i]);
 }
 
 __global__ void perm_vec_in_kernel(int n, const int32_t* perm, const double* in, double* out) {
@@ -1056,6 +1162,9 @@ struct RegFusion {
   T* b_store = nullptr;         // ... and stored here
   bool aout = false;            // post relax: b' = b - A_out x_in formed in the kernel
   double* z64 = nullptr;        // result widened to FP64 here instead of xout
+  const double* dot_r = nullptr;  // with z64: CTA partials of z.dot_r (and z.dot_o) to dot_part
+  const double* dot_o = nullptr;
+  double* dot_part = nullptr;
 };
 
 // The partition-block sweeps alone; a post relax reads its right-hand side b' =
@@ -1074,7 +1183,8 @@ void smooth_sweeps(Ctx& c, Level<T>& L, bool post, const T* b, const T* xin, T* 
     FG_LAUNCH(k, L.smooth_grid, L.smooth_threads, L.smooth_smem, s, L.ngroups, L.grows.p, L.Ain.rp.p, L.ci16.p,
               L.Ain.v.p, L.diag.p, L.dinv.p, b, w, inner, xin, xout, rout, L.max_group_ents + 16,
               c.red.p + 2 * kRedBlocks + S_KERR, f.b64, f.b_store, f.aout ? L.Aout.rp.p : nullptr,
-              f.aout ? L.Aout.ci.p : nullptr, f.aout ? L.Aout.v.p : nullptr, f.z64);
+              f.aout ? L.Aout.ci.p : nullptr, f.aout ? L.Aout.v.p : nullptr, f.z64, f.dot_r, f.dot_o, f.dot_part,
+              c.rcount.p + 3, c.red.p + 2 * kRedBlocks, f.dot_o ? 1 : 0);
     return;
   }
   if (L.smooth_k > 0) {
@@ -1112,6 +1222,12 @@ void smooth(Ctx& c, Level<T>& L, bool post, const T* b, const T* xin, T* xout, T
     f.b_store = post ? nullptr : b_store;
     f.aout = post && L.Aout.nnz > 0;
     f.z64 = z64;
+    if (z64 && c.zdot && L.smooth_grid <= kRedBlocks / 2) {
+      f.dot_r = c.zdot->r;
+      f.dot_o = c.zdot->rold;
+      f.dot_part = c.zdot->part;
+      c.zdot->done = true;
+    }
     smooth_sweeps<T>(c, L, post, b, xin, xout, rout, f);
     return;
   }
@@ -1225,7 +1341,7 @@ void ensure_work(Ctx& c, int n) {
   if (c.red.n == 0) {
     c.red.alloc(2 * kRedBlocks + 64, s);
     c.red.zero();
-    c.rcount.alloc(4, s);
+    c.rcount.alloc(8, s);
     c.rcount.zero();
   }
   if (!c.h_scalars) FG_CUDA(cudaMallocHost((void**)&c.h_scalars, 64 * sizeof(double)));
@@ -1427,9 +1543,21 @@ void pcg_iteration_body(Ctx& c, int n, int flexible, bool to_host) {
   double* part2 = c.red.p + kRedBlocks;
   double* sc = c.red.p + 2 * kRedBlocks;
   unsigned* cnt = c.rcount.p;
-  precondition_any(c, c.vr.p, c.vz.p);
-  FG_LAUNCH(dot_beta_kernel, kRedBlocks, kRedThreads, 0, s, n, c.vz.p, c.vr.p, flexible ? c.vrold.p : nullptr, part,
-            part2, sc, flexible, cnt);
+  Ctx::ZDot zd;
+  zd.r = c.vr.p;
+  zd.rold = flexible ? c.vrold.p : nullptr;
+  zd.part = part;
+  c.zdot = &zd;
+  try {
+    precondition_any(c, c.vr.p, c.vz.p);
+  } catch (...) {
+    c.zdot = nullptr;
+    throw;
+  }
+  c.zdot = nullptr;
+  if (!zd.done)  // else z.r (z.r_old) and beta came from the smoother that wrote z
+    FG_LAUNCH(dot_beta_kernel, kRedBlocks, kRedThreads, 0, s, n, c.vz.p, c.vr.p, flexible ? c.vrold.p : nullptr,
+              part, part2, sc, flexible, cnt);
   FG_LAUNCH(pupdate_kernel, kRedBlocks, kRedThreads, 0, s, n, sc, c.vz.p, c.vp.p);
   launch_spmv_dot(c, n, c.vp.p, c.vy.p);
   FG_LAUNCH(update_kernel, kRedBlocks, kRedThreads, 0, s, n, sc, c.vp.p, c.vy.p, c.vx.p, c.vr.p,
@@ -1530,6 +1658,8 @@ SolveResult amg_solve_device(Ctx& c, const double* d_b, double* d_x) {
   FG_LAUNCH(set_slot_kernel, 1, 1, 0, s, sc, S_FLAG, 0.0);
   FG_LAUNCH(set_slot_kernel, 1, 1, 0, s, sc, S_FIRST, 1.0);
   FG_LAUNCH(set_slot_kernel, 1, 1, 0, s, sc, S_KERR, 0.0);
+  // last-block tickets start at zero (a CTA that gave up on a copy leaves its ticket unset)
+  FG_CUDA(cudaMemsetAsync(c.rcount.p, 0, c.rcount.n * sizeof(unsigned), s));
   FG_CUDA(cudaMemsetAsync(c.vp.p, 0, n * sizeof(double), s));
   FG_CUDA(cudaMemcpyAsync(c.h_scalars, sc, S_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s));
   FG_CUDA(cudaStreamSynchronize(s));

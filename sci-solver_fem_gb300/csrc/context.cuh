@@ -145,6 +145,15 @@ struct Ctx {
   int graph_flexible = -1;
   cudaGraphExec_t pcg_exec = nullptr;
   int64_t graph_nodes = 0;
+  // z.r (and z.r_old) of the PCG iteration being enqueued, requested from the level-0
+  // post-smoother that writes z; `done` tells whether it took them (and formed beta)
+  struct ZDot {
+    const double* r = nullptr;
+    const double* rold = nullptr;
+    double* part = nullptr;
+    bool done = false;
+  };
+  ZDot* zdot = nullptr;
   // stage timing of a V-cycle run outside capture (FEMGPU_PROFILE set): named events
   std::vector<std::pair<std::string, cudaEvent_t>>* stage_marks = nullptr;
 
