@@ -1941,6 +1941,33 @@ void build_smoother_groups(Ctx& c, Level<T>& L, int max_rows, int max_ents) {
   L.grows.upload(g.data(), g.size());
 }
 
+// ci[e] = map[ci[e]]
+__global__ void map_columns_kernel(int64_t nnz, const int32_t* __restrict__ map, int32_t* ci) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < nnz) ci[e] = map[ci[e]];
+}
+
+// len[i] = length of row src[i] of rp
+__global__ void gather_row_lengths_kernel(int m, const int32_t* __restrict__ src, const int32_t* __restrict__ rp,
+                                          int32_t* __restrict__ len) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) len[i] = rp[src[i] + 1] - rp[src[i]];
+}
+
+// Row i of the output is row src[i] of the input (one warp per row, entries in order).
+template <class T>
+__global__ void gather_rows_kernel(int m, const int32_t* __restrict__ src, const int32_t* __restrict__ rp,
+                                   const int32_t* __restrict__ ci, const T* __restrict__ v,
+                                   const int32_t* __restrict__ orp, int32_t* __restrict__ oci, T* __restrict__ ov) {
+  const int i = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  if (i >= m) return;
+  const int a = rp[src[i]], len = rp[src[i] + 1] - a, o = orp[i];
+  for (int t = lane; t < len; t += 32) {
+    oci[o + t] = ci[a + t];
+    ov[o + t] = v[a + t];
+  }
+}
+
 template <class T>
 void build_levels(Ctx& c, Hierarchy<T>& H) {
   cudaStream_t s = c.stream;
@@ -2146,6 +2173,31 @@ void build_levels(Ctx& c, Hierarchy<T>& H) {
     num_levels++;
   }
   H.num_levels = num_levels;
+  // The V-cycle keeps every non-coarsest level's vectors in that level's own (permuted)
+  // order: each parent's restriction writes its rows in the child's order and its
+  // prolongation reads the child's vector by the child's new indices, so no separate
+  // permutation runs per cycle.  Entry order within each row is kept (same sums).
+  for (size_t l = 0; l + 1 < H.L.size(); l++) {
+    Level<T>& L = *H.L[l];
+    const Level<T>& N = *H.L[l + 1];
+    if (L.coarsest || N.coarsest) continue;
+    if (L.P.nnz > 0)
+      FG_LAUNCH(map_columns_kernel, grid_for(L.P.nnz, 256), 256, 0, s, L.P.nnz, N.perm.p, L.P.ci.p);
+    const int m = L.R.n;
+    DCsr<T> Rp;
+    Rp.n = m;
+    Rp.m = L.R.m;
+    Rp.nnz = L.R.nnz;
+    DBuf<int32_t> len(m + 1, s);
+    Rp.rp.alloc(m + 1, s);
+    FG_LAUNCH(gather_row_lengths_kernel, grid_for(m, 256), 256, 0, s, m, N.iperm.p, L.R.rp.p, len.p);
+    exclusive_scan(len.p, Rp.rp.p, m, s);
+    Rp.ci.alloc(L.R.nnz > 0 ? L.R.nnz : 1, s);
+    Rp.v.alloc(L.R.nnz > 0 ? L.R.nnz : 1, s);
+    FG_LAUNCH(gather_rows_kernel<T>, grid_for((int64_t)m * 32, 256), 256, 0, s, m, N.iperm.p, L.R.rp.p, L.R.ci.p,
+              L.R.v.p, Rp.rp.p, Rp.ci.p, Rp.v.p);
+    L.R = std::move(Rp);
+  }
 }
 
 __global__ void identity_kernel(int n, int32_t* p) {

@@ -52,18 +52,6 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
 
 // ---- level kernels -----------------------------------------------------------------
 template <class T>
-__global__ void permute_in_kernel(int n, const int32_t* iperm, const T* in, T* out) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) out[i] = in[iperm[i]];
-}
-
-template <class T>
-__global__ void permute_out_kernel(int n, const int32_t* iperm, const T* in, T* out) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) out[iperm[i]] = in[i];
-}
-
-template <class T>
 __global__ void cast_in_kernel(int n, const double* in, T* out) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = (T)in[i];
@@ -1267,12 +1255,7 @@ void vcycle(Ctx& c, Hierarchy<T>& H, int l, T* b_in, T* x_out, double* z_out = n
     stage_mark(c, "coarse", l);
     return;
   }
-  const T* b = b_in;
-  if (l > 0) {
-    FG_LAUNCH(permute_in_kernel<T>, grid_for(n, 256), 256, 0, s, n, L.iperm.p, b_in, L.b.p);
-    b = L.b.p;
-    stage_mark(c, "permute_in", l);
-  }
+  const T* b = b_in;  // already in this level's order (the parent's restriction writes it so)
   smooth<T>(c, L, false, b, nullptr, L.x.p, L.r.p, r64, b_in);
   stage_mark(c, "pre", l);
   aout_residual<T>(s, L, L.x.p, L.r.p);
@@ -1286,17 +1269,21 @@ void vcycle(Ctx& c, Hierarchy<T>& H, int l, T* b_in, T* x_out, double* z_out = n
   vcycle(c, H, l + 1, bc, xc);
   spmv_lanes(L.P, xc, L.x.p, 1, s);
   stage_mark(c, "prolong", l);
-  bool z_done = false;
+  bool z_done = false, out_done = false;
   for (int rl = 0; rl < c.cfg.postRelaxes; rl++) {
-    // the last post relax of level 0 writes z itself
-    double* z64 = (l == 0 && z_out && rl + 1 == c.cfg.postRelaxes) ? z_out : nullptr;
-    smooth<T>(c, L, true, b, L.x.p, L.r.p, nullptr, nullptr, nullptr, z64);
-    std::swap(L.x.p, L.r.p);  // r is free after the restriction: use it as the ping-pong buffer
+    const bool last = rl + 1 == c.cfg.postRelaxes;
+    // the last post relax of level 0 writes z itself; of a coarser level, x_out (this
+    // level's order, which the parent's prolongation reads)
+    double* z64 = (l == 0 && z_out && last) ? z_out : nullptr;
+    T* dst = (l > 0 && last) ? x_out : L.r.p;
+    smooth<T>(c, L, true, b, L.x.p, dst, nullptr, nullptr, nullptr, z64);
+    if (dst == L.r.p) std::swap(L.x.p, L.r.p);  // r is free after the restriction: the ping-pong buffer
     z_done = z64 != nullptr;
+    out_done = dst == x_out;
   }
   stage_mark(c, "post", l);
   if (l > 0) {
-    FG_LAUNCH(permute_out_kernel<T>, grid_for(n, 256), 256, 0, s, n, L.iperm.p, L.x.p, x_out);
+    if (!out_done) FG_CUDA(cudaMemcpyAsync(x_out, L.x.p, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
   } else if (z_out) {
     if (!z_done) FG_LAUNCH(cast_out_kernel<T>, grid_for(n, 256), 256, 0, s, n, L.x.p, z_out);
   } else {

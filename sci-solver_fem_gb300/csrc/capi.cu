@@ -118,6 +118,15 @@ void get_level(Ctx& c, int level, int32_t* Arp, int32_t* Aci, double* Av, int32_
     if (Pv) copy_vals(L.P.v, L.P.nnz, Pv);
   }
   FG_CUDA(cudaStreamSynchronize(s));
+  // P's columns are kept in the next level's own order when that level is not the
+  // coarsest; report them in its original (aggregate) numbering
+  if (!L.coarsest && Pci && level + 1 < c.H->num_levels) {
+    const Level<T>& N = level_of<T>(c, level + 1);
+    if (!N.coarsest) {
+      std::vector<int32_t> ip = N.iperm.to_host();
+      for (int64_t e = 0; e < L.P.nnz; e++) Pci[e] = ip[Pci[e]];
+    }
+  }
 }
 
 }  // namespace
