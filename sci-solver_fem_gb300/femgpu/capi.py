@@ -267,8 +267,8 @@ class Solver:
         return dict(status=status, iterations=st.iterations, relres=st.relative_residual,
                     setup_ms=st.setup_ms, solve_ms=st.solve_ms, levels=st.num_levels)
 
-    KERNELS = {0: "spmv_dot_kernel (FP64 CSR outer SpMV + dot)", 1: "smooth pre (level 0)", 2: "smooth post (level 0)",
-               3: "spmv_lanes R (level 0)", 4: "spmv_lanes P (level 0)"}
+    KERNELS = {0: "spmv_dot_sliced_kernel (FP64 outer SpMV + dot, 32-row slices)", 1: "smooth pre (level 0)",
+               2: "smooth post (level 0)", 3: "spmv_lanes R (level 0)", 4: "spmv_lanes P (level 0)"}
 
     def profile_kernel(self, which: int, reps: int = 20):
         ms, nb = C.c_double(), C.c_double()
