@@ -346,11 +346,12 @@ __global__ void swap_kernel(int np, unsigned long long* best, int32_t* part, con
 }
 
 // removeRuntyParts / removeRuntyPartitions (misHelpers.cu:744-820).  Returns the
-// number of removed parts.
+// number of removed parts.  np: the number of parts (labels 0 .. np-1, none empty)
+// when the caller tracks it, else -1 (then it is read from the labels).
 int remove_small_parts(Ctx& c, int n, DBuf<int32_t>& part, const int32_t* weights, int threshold_mode, int min_size,
-                       int full_size, DBuf<int32_t>& aggregated) {
+                       int full_size, DBuf<int32_t>& aggregated, int np = -1) {
   cudaStream_t s = c.stream;
-  int np = reduce_max(part.p, n, s) + 1;
+  if (np < 0) np = reduce_max(part.p, n, s) + 1;
   DBuf<int32_t> sizes(np, s), rm(np + 1, s), sub(np + 1, s);
   sizes.zero();
   FG_LAUNCH(histogram_kernel, grid_for(n, 256), 256, 0, s, n, part.p, weights, sizes.p);
@@ -388,9 +389,11 @@ int restrict_partitions(Ctx& c, int max_size, int full_size, int n, const int32_
   return np;
 }
 
-// aggregateGraph / aggregateWeightedGraph (misHelpers.cu:513-677).
-void aggregate(Ctx& c, int n, const int32_t* xadj, const int32_t* adj, int depth, bool weighted, int min_size,
-               int max_size, int full_size, const int32_t* weights, DBuf<int32_t>& part) {
+// aggregateGraph / aggregateWeightedGraph (misHelpers.cu:513-677).  Returns the number
+// of parts for the unweighted graph (the parts are labelled 0 .. count-1), -1 for the
+// weighted one (whose partition restriction may empty a part).
+int aggregate(Ctx& c, int n, const int32_t* xadj, const int32_t* adj, int depth, bool weighted, int min_size,
+              int max_size, int full_size, const int32_t* weights, DBuf<int32_t>& part) {
   cudaStream_t s = c.stream;
   PhaseTimer pt(s, -4);
   DBuf<int32_t> mis;
@@ -399,7 +402,9 @@ void aggregate(Ctx& c, int n, const int32_t* xadj, const int32_t* adj, int depth
   DBuf<int32_t> incl(n + 1, s), aggregated(n, s), pout(n, s), counters(2, s);
   FG_CUDA(cudaMemcpyAsync(incl.p, mis.p, n * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
   inclusive_scan_inplace(incl.p, n, s);
-  int mis_count = read_scalar(incl.p + (n - 1), s);
+  // the MIS size (= the number of parts, labelled 0 .. count-1 by label_roots_kernel)
+  // comes back with the first allocation counters
+  int mis_count = -1;
   part.alloc(n, s);
   FG_LAUNCH(label_roots_kernel, grid_for(n, 256), 256, 0, s, n, mis.p, incl.p, part.p, aggregated.p);
   bool first = true;
@@ -415,24 +420,32 @@ void aggregate(Ctx& c, int n, const int32_t* xadj, const int32_t* adj, int depth
     }
     int32_t h[2];
     counters.download(h, 2);
+    if (mis_count < 0 && n > 0) FG_CUDA(cudaMemcpyAsync(&mis_count, incl.p + (n - 1), sizeof(int32_t),
+                                                       cudaMemcpyDeviceToHost, s));
     FG_CUDA(cudaStreamSynchronize(s));
     g_host_syncs.fetch_add(1, std::memory_order_relaxed);
+    if (mis_count < 0) mis_count = 0;
     pt.mark("allocate");
     if (h[0] == 0) {
       if (!weighted) {
-        if (remove_small_parts(c, n, part, nullptr, 0, min_size, full_size, aggregated) == 0) return;
+        // unweighted parts are never emptied: their count is tracked, not read back
+        const int removed = remove_small_parts(c, n, part, nullptr, 0, min_size, full_size, aggregated, mis_count);
+        if (removed == 0) return mis_count;
+        mis_count -= removed;
       } else {
         if (!first || mis_count < 10) {
           restrict_partitions(c, max_size, full_size, n, xadj, adj, part, weights);
-          return;
+          return -1;
         }
         first = false;
         remove_small_parts(c, n, part, weights, 1, 0, full_size, aggregated);
       }
-      FG_REQUIRE(count_equal(aggregated.p, n, 1, s) > 0, FEMGPU_ERR_LIMIT,
-                 "every aggregate was removed as undersized (the reference loops forever here)");
     } else if (h[1] == 0) {
-      throw Error(FEMGPU_ERR_LIMIT, "aggregation stalled: nodes unreachable from any aggregate");
+      // also the case where every aggregate was removed as undersized (the reference
+      // loops forever there)
+      throw Error(FEMGPU_ERR_LIMIT,
+                  "aggregation stalled: nodes unreachable from any aggregate, or every aggregate was removed "
+                  "as undersized");
     }
   }
 }
@@ -627,14 +640,13 @@ void old_mis(Ctx& c, int n, const int32_t* xadj, const int32_t* adj, OldMisOut& 
   const int fine_depth = params % 100, coarse_depth = (params / 100) % 100, min_agg = (params / 10000) % 10;
   PhaseTimer pt(s, -1);
   DBuf<int32_t> fine;
-  aggregate(c, n, xadj, adj, fine_depth, false, min_agg, 0, n, nullptr, fine);
+  const int nagg = aggregate(c, n, xadj, adj, fine_depth, false, min_agg, 0, n, nullptr, fine);
   pt.mark("fine agg");
-  const int nagg = reduce_max(fine.p, n, s) + 1;
   // aggregate member lists, ascending node id
   DBuf<int32_t> acount(nagg + 1, s), astart(nagg + 1, s), cursor(nagg, s), members(n, s);
   acount.zero();
   FG_LAUNCH(histogram_kernel, grid_for(n, 256), 256, 0, s, n, fine.p, nullptr, acount.p);
-  exclusive_scan(acount.p, astart.p, nagg, s);
+  exclusive_scan_async(acount.p, astart.p, nagg, s);
   cursor.zero();
   FG_LAUNCH(scatter_bucket_kernel, grid_for(n, 256), 256, 0, s, n, fine.p, astart.p, cursor.p, members.p);
   segmented_sort_i32(members.p, astart.p, nagg, nullptr, s);
@@ -642,15 +654,24 @@ void old_mis(Ctx& c, int n, const int32_t* xadj, const int32_t* adj, OldMisOut& 
   DBuf<int32_t> ucount(nagg + 1, s), ixadj(nagg + 1, s), iadj;
   DBuf<int32_t> mdeg(n + 1, s), noff(n + 1, s);
   FG_LAUNCH(member_degree_kernel, grid_for(n, 256), 256, 0, s, n, members.p, xadj, mdeg.p);
-  exclusive_scan(mdeg.p, noff.p, n, s);
+  exclusive_scan_async(mdeg.p, noff.p, n, s);
   bool induced_done = false;
+  int64_t induced_nnz = 0;
   {
     DBuf<int32_t> tmp((size_t)nagg * kIndCap, s), ovf(1, s);
     ovf.zero();
     FG_LAUNCH(induced_hash_kernel, (int)std::min<int64_t>((nagg + 7) / 8, 152 * 16), 256, 0, s, nagg, astart.p,
               members.p, noff.p, xadj, adj, fine.p, tmp.p, ucount.p, ovf.p);
-    if (read_scalar(ovf.p, s) == 0) {
-      const int64_t innz = exclusive_scan(ucount.p, ixadj.p, nagg, s);
+    // the overflow flag and the total come back in one round trip
+    exclusive_scan_async(ucount.p, ixadj.p, nagg, s);
+    int32_t h_ovf = 0, h_tot = 0;
+    FG_CUDA(cudaMemcpyAsync(&h_ovf, ovf.p, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    FG_CUDA(cudaMemcpyAsync(&h_tot, ixadj.p + nagg, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    FG_CUDA(cudaStreamSynchronize(s));
+    g_host_syncs.fetch_add(1, std::memory_order_relaxed);
+    if (h_ovf == 0) {
+      const int64_t innz = h_tot;
+      induced_nnz = innz;
       iadj.alloc(innz > 0 ? innz : 1, s);
       FG_LAUNCH(compact_stride_kernel, grid_for((int64_t)nagg * 32, 256), 256, 0, s, nagg, tmp.p, kIndCap, ixadj.p,
                 iadj.p);
@@ -669,6 +690,7 @@ void old_mis(Ctx& c, int n, const int32_t* xadj, const int32_t* adj, OldMisOut& 
     segmented_sort_i32(cand.p, coff.p, nagg, ucount.p, s);
     FG_LAUNCH(drop_padding_kernel, grid_for(nagg, 256), 256, 0, s, nagg, coff.p, ucount.p, cand.p);
     int64_t innz = exclusive_scan(ucount.p, ixadj.p, nagg, s);
+    induced_nnz = innz;
     iadj.alloc(innz > 0 ? innz : 1, s);
     FG_LAUNCH(compact_segments_kernel, grid_for((int64_t)nagg * 32, 256), 256, 0, s, nagg, cand.p, coff.p, ixadj.p,
               iadj.p);
@@ -684,7 +706,7 @@ void old_mis(Ctx& c, int n, const int32_t* xadj, const int32_t* adj, OldMisOut& 
   pcount.zero();
   FG_LAUNCH(histogram_kernel, grid_for(nagg, 256), 256, 0, s, nagg, coarse.p, nullptr, pcount.p);
   o.part_idx.alloc(npart + 1, s);
-  exclusive_scan(pcount.p, o.part_idx.p, npart, s);
+  exclusive_scan_async(pcount.p, o.part_idx.p, npart, s);
   pcur.zero();
   FG_LAUNCH(scatter_bucket_kernel, grid_for(nagg, 256), 256, 0, s, nagg, coarse.p, o.part_idx.p, pcur.p, old_of.p);
   segmented_sort_i32(old_of.p, o.part_idx.p, npart, nullptr, s);
@@ -694,7 +716,8 @@ void old_mis(Ctx& c, int n, const int32_t* xadj, const int32_t* adj, OldMisOut& 
   DBuf<int32_t> rlen(nagg + 1, s);
   FG_LAUNCH(gather_len_kernel, grid_for(nagg, 256), 256, 0, s, nagg, old_of.p, ixadj.p, rlen.p);
   o.xadj_out.alloc(nagg + 1, s);
-  o.nnz_out = exclusive_scan(rlen.p, o.xadj_out.p, nagg, s);
+  exclusive_scan_async(rlen.p, o.xadj_out.p, nagg, s);
+  o.nnz_out = induced_nnz;  // the same rows, reordered
   o.adj_out.alloc(o.nnz_out > 0 ? o.nnz_out : 1, s);
   FG_LAUNCH(remap_graph_kernel, grid_for(nagg, 256), 256, 0, s, nagg, old_of.p, ixadj.p, iadj.p, new_id.p,
             o.xadj_out.p, o.adj_out.p);
@@ -702,7 +725,7 @@ void old_mis(Ctx& c, int n, const int32_t* xadj, const int32_t* adj, OldMisOut& 
   DBuf<int32_t> asz(nagg + 1, s);
   FG_LAUNCH(gather_len_kernel, grid_for(nagg, 256), 256, 0, s, nagg, old_of.p, astart.p, asz.p);
   o.agg_idx.alloc(nagg + 1, s);
-  exclusive_scan(asz.p, o.agg_idx.p, nagg, s);
+  exclusive_scan_async(asz.p, o.agg_idx.p, nagg, s);
   o.iperm.alloc(n, s);
   o.perm.alloc(n, s);
   o.agg_of.alloc(n, s);
@@ -2123,7 +2146,7 @@ void build_levels(Ctx& c, Hierarchy<T>& H) {
       cur.zero();
       FG_LAUNCH(transpose_count_kernel<T>, grid_for(L.P.nnz, 256), 256, 0, s, L.P.nnz, L.P.ci.p, cnt.p);
       Ru.rp.alloc(L.nagg + 1, s);
-      exclusive_scan(cnt.p, Ru.rp.p, L.nagg, s);
+      exclusive_scan_async(cnt.p, Ru.rp.p, L.nagg, s);
       Ru.ci.alloc(L.P.nnz, s);
       Ru.v.alloc(L.P.nnz, s);
       FG_LAUNCH(transpose_fill_kernel<T>, grid_for(N, 256), 256, 0, s, N, L.P.rp.p, L.P.ci.p, L.P.v.p, Ru.rp.p, cur.p,
@@ -2191,7 +2214,7 @@ void build_levels(Ctx& c, Hierarchy<T>& H) {
     DBuf<int32_t> len(m + 1, s);
     Rp.rp.alloc(m + 1, s);
     FG_LAUNCH(gather_row_lengths_kernel, grid_for(m, 256), 256, 0, s, m, N.iperm.p, L.R.rp.p, len.p);
-    exclusive_scan(len.p, Rp.rp.p, m, s);
+    exclusive_scan_async(len.p, Rp.rp.p, m, s);
     Rp.ci.alloc(L.R.nnz > 0 ? L.R.nnz : 1, s);
     Rp.v.alloc(L.R.nnz > 0 ? L.R.nnz : 1, s);
     FG_LAUNCH(gather_rows_kernel<T>, grid_for((int64_t)m * 32, 256), 256, 0, s, m, N.iperm.p, L.R.rp.p, L.R.ci.p,

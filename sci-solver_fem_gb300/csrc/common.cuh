@@ -147,6 +147,8 @@ inline T read_scalar(const T* d, cudaStream_t s) {
 // Exclusive scan of n int32 counts into out[0..n] (out[n] = total, int64 safe
 // total returned).  out may alias in only if in has n+1 entries.
 int64_t exclusive_scan(const int32_t* in, int32_t* out, int64_t n, cudaStream_t s);
+// The same scan with the total left on the device (out[n]); no host round trip.
+void exclusive_scan_async(const int32_t* in, int32_t* out, int64_t n, cudaStream_t s);
 // Inclusive scan in place.
 void inclusive_scan_inplace(int32_t* a, int64_t n, cudaStream_t s);
 int32_t reduce_max(const int32_t* a, int64_t n, cudaStream_t s);

@@ -268,7 +268,7 @@ __global__ void seg_len_kernel(const int32_t* off, int nseg, int32_t* out) {
 
 }  // namespace
 
-int64_t exclusive_scan(const int32_t* in, int32_t* out, int64_t n, cudaStream_t s) {
+void exclusive_scan_async(const int32_t* in, int32_t* out, int64_t n, cudaStream_t s) {
   DBuf<int32_t> last(1, s);
   if (n > 0) {
     copy_one_kernel<<<1, 32, 0, s>>>(in + (n - 1), last.p);
@@ -277,13 +277,17 @@ int64_t exclusive_scan(const int32_t* in, int32_t* out, int64_t n, cudaStream_t 
   exclusive_scan_rec(in, out, n, s);
   write_total_kernel<<<1, 32, 0, s>>>(out, n, last.p, n > 0);
   FG_CHECK_LAUNCH();
+}
+
+int64_t exclusive_scan(const int32_t* in, int32_t* out, int64_t n, cudaStream_t s) {
+  exclusive_scan_async(in, out, n, s);
   return (int64_t)read_scalar(out + n, s);
 }
 
 void inclusive_scan_inplace(int32_t* a, int64_t n, cudaStream_t s) {
   if (n <= 0) return;
   DBuf<int32_t> tmp(n + 1, s);
-  exclusive_scan(a, tmp.p, n, s);
+  exclusive_scan_async(a, tmp.p, n, s);
   // inclusive[i] = exclusive[i+1]
   FG_CUDA(cudaMemcpyAsync(a, tmp.p + 1, n * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
 }
