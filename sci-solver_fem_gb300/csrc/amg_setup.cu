@@ -1167,10 +1167,15 @@ void run_esc_sort(Ctx& c, EscArgs<T> a, int nrows_out, int ncols_out, DCsr<T>& o
             kEscBlockCap, big.p, nbig.p);
   FG_LAUNCH(collect_dense_rows_kernel, grid_for(nrows_out, 256), 256, 0, s, nrows_out, items.p, kEscBlockCap,
             dense.p, ndense.p);
-  a.nbig = read_scalar(nbig.p, s);
+  int32_t h_big = 0, h_dense = 0;  // both counts in one round trip
+  FG_CUDA(cudaMemcpyAsync(&h_big, nbig.p, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  FG_CUDA(cudaMemcpyAsync(&h_dense, ndense.p, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  FG_CUDA(cudaStreamSynchronize(s));
+  g_host_syncs.fetch_add(1, std::memory_order_relaxed);
+  a.nbig = h_big;
   a.big_rows = big.p;
   EscArgs<T> ad = a;  // dense tier: rows with more items than the sort capacity
-  ad.nbig = read_scalar(ndense.p, s);
+  ad.nbig = h_dense;
   ad.big_rows = dense.p;
   const int dgrid = std::min(ad.nbig, 152 * 2);
   const size_t dsm = (size_t)ncols_out * (sizeof(T) + 1);
@@ -1618,7 +1623,19 @@ void run_spgemm_hash(Ctx& c, EscArgs<T> a, int nrows_out, int ncols_out, DCsr<T>
               (const int32_t*)nullptr, toff.p, tci.p, tv.p, cnt.p, over1.p, nover1.p);
   }
   pt.mark("sp rows");
-  const int n1 = read_scalar(nover1.p, s);
+  // the output offsets are scanned before the overflow count is read, so when no row
+  // overflowed (the usual case) both come back in one round trip
+  out.n = nrows_out;
+  out.m = ncols_out;
+  out.rp.alloc(nrows_out + 1, s);
+  exclusive_scan_async(cnt.p, out.rp.p, nrows_out, s);
+  int32_t h_n1 = 0, h_tot = 0;
+  FG_CUDA(cudaMemcpyAsync(&h_n1, nover1.p, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  FG_CUDA(cudaMemcpyAsync(&h_tot, out.rp.p + nrows_out, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  FG_CUDA(cudaStreamSynchronize(s));
+  g_host_syncs.fetch_add(1, std::memory_order_relaxed);
+  const int n1 = h_n1;
+  out.nnz = h_tot;
   if (n1 > 0) {
     const size_t bsm = (size_t)kHashBlockCap * (sizeof(unsigned long long) + sizeof(T) + sizeof(int32_t));
     ensure_smem(hash_block_kernel<T>, bsm);
@@ -1645,12 +1662,9 @@ void run_spgemm_hash(Ctx& c, EscArgs<T> a, int nrows_out, int ncols_out, DCsr<T>
       FG_LAUNCH((esc_dense_kernel<T, ESC_SPGEMM, true>), std::min(n2, 304), 256, dsm, s, ad, ncols_out, nullptr,
                 nullptr);
     }
+    out.nnz = exclusive_scan(cnt.p, out.rp.p, nrows_out, s);  // the overflow rows' counts are in now
   }
   pt.mark("sp big");
-  out.n = nrows_out;
-  out.m = ncols_out;
-  out.rp.alloc(nrows_out + 1, s);
-  out.nnz = exclusive_scan(cnt.p, out.rp.p, nrows_out, s);
   out.ci.alloc(out.nnz > 0 ? out.nnz : 1, s);
   out.v.alloc(out.nnz > 0 ? out.nnz : 1, s);
   FG_LAUNCH(compact_rows_copy_kernel<T>, grid_for((int64_t)nrows_out * 32, 256), 256, 0, s, nrows_out, toff.p, tci.p,
@@ -1945,7 +1959,11 @@ void build_smoother_groups(Ctx& c, Level<T>& L, int max_rows, int max_ents) {
   DBuf<int32_t> row0(L.npart + 1, s), ent0(L.npart + 1, s);
   FG_LAUNCH(partition_starts_kernel, grid_for(L.npart + 1, 256), 256, 0, s, L.npart, L.part_idx.p, L.agg_idx.p,
             L.Ain.rp.p, row0.p, ent0.p);
-  std::vector<int32_t> hr = row0.to_host(), he = ent0.to_host();
+  std::vector<int32_t> hr(L.npart + 1), he(L.npart + 1);
+  row0.download(hr.data(), L.npart + 1);
+  ent0.download(he.data(), L.npart + 1);
+  FG_CUDA(cudaStreamSynchronize(s));
+  g_host_syncs.fetch_add(1, std::memory_order_relaxed);
   std::vector<int32_t> g{hr[0]};
   int gp = 0, mx = 0, mxe = 0;
   for (int p = 1; p <= L.npart; p++) {
@@ -2072,16 +2090,34 @@ void build_levels(Ctx& c, Hierarchy<T>& H) {
     FG_LAUNCH(diag_kernel<T>, grid_for(N, 256), 256, 0, s, N, L.Ap.rp.p, L.Ap.ci.p, L.Ap.v.p, L.diag.p);
     L.dinv.alloc(N, s);
     FG_LAUNCH(reciprocal_kernel<T>, grid_for(N, 256), 256, 0, s, N, L.diag.p, L.dinv.p);
-    // in/out-of-partition split
+    // in/out-of-partition split; the two entry counts and the three maxima the smoother
+    // plan needs come back in one round trip
     {
-      DBuf<int32_t> cin(N + 1, s), cout(N + 1, s);
+      DBuf<int32_t> cin(N + 1, s), cout(N + 1, s), prow(L.npart + 1, s), pent(L.npart + 1, s), mx(3, s);
       FG_LAUNCH(split_count_kernel<T>, grid_for(N, 256), 256, 0, s, N, L.Ap.rp.p, L.Ap.ci.p, o.part_of_row.p, cin.p,
                 cout.p);
       L.Ain.n = L.Ain.m = L.Aout.n = L.Aout.m = N;
       L.Ain.rp.alloc(N + 1, s);
       L.Aout.rp.alloc(N + 1, s);
-      L.Ain.nnz = exclusive_scan(cin.p, L.Ain.rp.p, N, s);
-      L.Aout.nnz = exclusive_scan(cout.p, L.Aout.rp.p, N, s);
+      reduce_max_async(cin.p, N, mx.p + 2, s);  // longest in-partition row
+      exclusive_scan_async(cin.p, L.Ain.rp.p, N, s);
+      exclusive_scan_async(cout.p, L.Aout.rp.p, N, s);
+      FG_LAUNCH(partition_rows_kernel, grid_for(L.npart, 256), 256, 0, s, L.npart, L.part_idx.p, L.agg_idx.p, prow.p);
+      reduce_max_async(prow.p, L.npart, mx.p, s);
+      FG_LAUNCH(partition_entries_kernel, grid_for(L.npart, 256), 256, 0, s, L.npart, L.part_idx.p, L.agg_idx.p,
+                L.Ain.rp.p, pent.p);
+      reduce_max_async(pent.p, L.npart, mx.p + 1, s);
+      int32_t h_in = 0, h_out = 0, h_mx[3] = {0, 0, 0};
+      FG_CUDA(cudaMemcpyAsync(&h_in, L.Ain.rp.p + N, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+      FG_CUDA(cudaMemcpyAsync(&h_out, L.Aout.rp.p + N, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+      FG_CUDA(cudaMemcpyAsync(h_mx, mx.p, 3 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+      FG_CUDA(cudaStreamSynchronize(s));
+      g_host_syncs.fetch_add(1, std::memory_order_relaxed);
+      L.Ain.nnz = h_in;
+      L.Aout.nnz = h_out;
+      L.max_part_rows = h_mx[0];
+      L.max_part_entries = h_mx[1];
+      L.max_in_row = h_mx[2];
       L.Ain.ci.alloc(L.Ain.nnz > 0 ? L.Ain.nnz : 1, s);
       L.Ain.v.alloc(L.Ain.nnz + 16, s);  // slack for 16-byte rounded bulk copies
       L.Ain.v.zero();
@@ -2091,15 +2127,6 @@ void build_levels(Ctx& c, Hierarchy<T>& H) {
                 o.part_of_row.p, L.Ain.rp.p, L.Ain.ci.p, L.Ain.v.p, L.Aout.rp.p, L.Aout.ci.p, L.Aout.v.p);
     }
     {
-      DBuf<int32_t> prow(L.npart + 1, s), pent(L.npart + 1, s);
-      FG_LAUNCH(partition_rows_kernel, grid_for(L.npart, 256), 256, 0, s, L.npart, L.part_idx.p, L.agg_idx.p, prow.p);
-      L.max_part_rows = reduce_max(prow.p, L.npart, s);
-      FG_LAUNCH(partition_entries_kernel, grid_for(L.npart, 256), 256, 0, s, L.npart, L.part_idx.p, L.agg_idx.p,
-                L.Ain.rp.p, pent.p);
-      L.max_part_entries = reduce_max(pent.p, L.npart, s);
-      DBuf<int32_t> rlen(N + 1, s);
-      FG_LAUNCH(row_lengths_kernel, grid_for(N, 256), 256, 0, s, N, L.Ain.rp.p, rlen.p);
-      L.max_in_row = reduce_max(rlen.p, N, s);
       pt.mark("split rows");
       if (smoother_in_registers(L.max_in_row, L.max_part_rows)) {
         build_smoother_groups(c, L, kRegGroupRows, std::numeric_limits<int>::max());

@@ -152,6 +152,8 @@ void exclusive_scan_async(const int32_t* in, int32_t* out, int64_t n, cudaStream
 // Inclusive scan in place.
 void inclusive_scan_inplace(int32_t* a, int64_t n, cudaStream_t s);
 int32_t reduce_max(const int32_t* a, int64_t n, cudaStream_t s);
+// The same maximum written to out[0] on the device (INT32_MIN when n == 0).
+void reduce_max_async(const int32_t* a, int64_t n, int32_t* out, cudaStream_t s);
 int64_t count_equal(const int32_t* a, int64_t n, int32_t value, cudaStream_t s);
 void fill_i32(int32_t* a, int64_t n, int32_t v, cudaStream_t s);
 void iota_i32(int32_t* a, int64_t n, cudaStream_t s);

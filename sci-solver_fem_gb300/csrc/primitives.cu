@@ -292,6 +292,14 @@ void inclusive_scan_inplace(int32_t* a, int64_t n, cudaStream_t s) {
   FG_CUDA(cudaMemcpyAsync(a, tmp.p + 1, n * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
 }
 
+void reduce_max_async(const int32_t* a, int64_t n, int32_t* out, cudaStream_t s) {
+  fill_i32(out, 1, INT32_MIN, s);
+  if (n > 0) {
+    reduce_max_kernel<<<reduce_grid(n), 256, 0, s>>>(a, n, out);
+    FG_CHECK_LAUNCH();
+  }
+}
+
 int32_t reduce_max(const int32_t* a, int64_t n, cudaStream_t s) {
   DBuf<int32_t> out(1, s);
   fill_i32(out.p, 1, INT32_MIN, s);
