@@ -774,6 +774,7 @@ struct EscArgs {
   T* ov;
   int32_t* overflow;
   int thread_cap;        // rows with at most this many items use the thread tier
+  int64_t known_nnz;     // PERMUTE: the input's entry count (every entry is kept), else 0
 };
 
 constexpr int kEscWarpCap = 1024;
@@ -1222,7 +1223,12 @@ void run_esc_sort(Ctx& c, EscArgs<T> a, int nrows_out, int ncols_out, DCsr<T>& o
   out.n = nrows_out;
   out.m = ncols_out;
   out.rp.alloc(nrows_out + 1, s);
-  out.nnz = exclusive_scan(MODE == ESC_PERMUTE ? items.p : ucnt.p, out.rp.p, nrows_out, s);
+  if (MODE == ESC_PERMUTE && a.known_nnz > 0) {  // a permutation keeps every entry: no read-back
+    exclusive_scan_async(items.p, out.rp.p, nrows_out, s);
+    out.nnz = a.known_nnz;
+  } else {
+    out.nnz = exclusive_scan(MODE == ESC_PERMUTE ? items.p : ucnt.p, out.rp.p, nrows_out, s);
+  }
   out.ci.alloc(out.nnz > 0 ? out.nnz : 1, s);
   out.v.alloc(out.nnz > 0 ? out.nnz : 1, s);
   a.orp = out.rp.p;
@@ -2083,6 +2089,7 @@ void build_levels(Ctx& c, Hierarchy<T>& H) {
       a.av = L.A.v.p;
       a.perm = L.perm.p;
       a.iperm = L.iperm.p;
+      a.known_nnz = L.A.nnz;
       run_esc<T, ESC_PERMUTE>(c, a, N, N, L.Ap);
     }
     pt.mark("permute");
@@ -2182,6 +2189,7 @@ void build_levels(Ctx& c, Hierarchy<T>& H) {
       a.arp = Ru.rp.p;
       a.aci = Ru.ci.p;
       a.av = Ru.v.p;
+      a.known_nnz = L.P.nnz;
       run_esc<T, ESC_PERMUTE>(c, a, L.nagg, N, L.R);
     }
     // Galerkin product A_next = R (Ap P)
