@@ -151,6 +151,17 @@ femgpu_status femgpu_solve_multi(femgpu_handle h, int nrhs, const double* B, dou
 femgpu_status femgpu_solve_multi_device(femgpu_handle h, int nrhs, const double* d_B, int64_t ldb, double* d_X,
                                        int64_t ldx, femgpu_solve_stats* stats);
 
+/* Independent problems at once: for each i, femgpu_setup(h[i]) when setup != 0, then
+ * femgpu_solve(h[i], b[i], x[i], &stats[i]) (host arrays, each the size of its own
+ * operator).  The handles must be distinct, each with its own stream (the default);
+ * they run on up to `threads` host threads (0: one per handle), so the small problems'
+ * setup round trips overlap and their kernels share the GPU.  Every problem is
+ * attempted; the first failing status (in index order) is returned, and each failing
+ * handle's femgpu_last_error names its problem.  stats may be NULL.
+ * No reference counterpart (the reference solves one mesh per FEMSolver). */
+femgpu_status femgpu_solve_batch(int count, femgpu_handle* h, const double* const* b, double* const* x, int setup,
+                                 int threads, femgpu_solve_stats* stats);
+
 /* Same as femgpu_solve with device pointers on the handle's stream (no copies). */
 femgpu_status femgpu_solve_device(femgpu_handle h, const double* d_b, double* d_x,
                                   femgpu_solve_stats* stats);

@@ -4,8 +4,11 @@
 // a status code (the reference calls exit() on bad input, gauss_seidel.cu:2060-2064;
 // tetmesh.cu:257-260); the message is kept on the handle (femgpu_last_error).
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <functional>
+#include <thread>
+#include <vector>
 
 #include "context.cuh"
 
@@ -466,6 +469,39 @@ femgpu_status femgpu_solve_multi(femgpu_handle h, int nrhs, const double* B, dou
     FG_CUDA(cudaStreamSynchronize(h->stream));
   });
   return st != FEMGPU_OK ? st : result;
+}
+
+femgpu_status femgpu_solve_batch(int count, femgpu_handle* hs, const double* const* b, double* const* x, int setup,
+                                 int threads, femgpu_solve_stats* stats) {
+  if (count < 0 || threads < 0) return FEMGPU_ERR_INVALID;
+  if (count == 0) return FEMGPU_OK;
+  if (!hs || !b || !x) return FEMGPU_ERR_INVALID;
+  std::vector<femgpu_handle> seen(hs, hs + count);
+  for (int i = 0; i < count; i++)
+    if (!hs[i] || !b[i] || !x[i]) return FEMGPU_ERR_INVALID;
+  std::sort(seen.begin(), seen.end());
+  if (std::adjacent_find(seen.begin(), seen.end()) != seen.end()) return FEMGPU_ERR_INVALID;  // one thread per handle
+  std::vector<femgpu_status> status(count, FEMGPU_OK);
+  std::atomic<int> next{0};
+  auto work = [&]() {
+    for (int i = next.fetch_add(1); i < count; i = next.fetch_add(1)) {
+      femgpu_status st = setup ? femgpu_setup(hs[i]) : FEMGPU_OK;
+      if (st == FEMGPU_OK) st = femgpu_solve(hs[i], b[i], x[i], stats ? &stats[i] : nullptr);
+      status[i] = st;
+    }
+  };
+  const int nt = threads == 0 ? count : std::min(threads, count);
+  std::vector<std::thread> pool;
+  try {
+    for (int t = 1; t < nt; t++) pool.emplace_back(work);
+  } catch (...) {
+    // fewer threads than asked (the remaining work is shared by the ones running)
+  }
+  work();
+  for (auto& t : pool) t.join();
+  for (int i = 0; i < count; i++)
+    if (status[i] != FEMGPU_OK) return status[i];
+  return FEMGPU_OK;
 }
 
 femgpu_status femgpu_adjoint_grad_device(femgpu_handle h, const double* d_dLdu, const double* d_u,

@@ -16,8 +16,8 @@ Typical use (the FEMSolver flow of the reference, src/FEMSolver.cu:9-93):
 from __future__ import annotations
 
 from .capi import (FemgpuError, Solver, native_library_path, kernel_launches, read_tetgen, read_ply,
-                   read_mat_sparse, read_mat_array, write_mat_array, write_vtk, STATUS)
+                   read_mat_sparse, read_mat_array, write_mat_array, write_vtk, STATUS, solve_batch)
 from . import meshes
 
 __all__ = ["FemgpuError", "Solver", "meshes", "native_library_path", "kernel_launches", "read_tetgen",
-           "read_ply", "read_mat_sparse", "read_mat_array", "write_mat_array", "write_vtk", "STATUS"]
+           "read_ply", "read_mat_sparse", "read_mat_array", "write_mat_array", "write_vtk", "STATUS", "solve_batch"]

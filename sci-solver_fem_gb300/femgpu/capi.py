@@ -26,7 +26,7 @@ EXPORTS = [
     "femgpu_setup", "femgpu_solve", "femgpu_solve_device", "femgpu_spmv_device", "femgpu_get_matrix",
     "femgpu_num_levels", "femgpu_get_level_info", "femgpu_level_get", "femgpu_vcycle", "femgpu_kernel_launches",
     "femgpu_profile_kernel", "femgpu_load_vector_device_noalloc", "femgpu_adjoint_grad",
-    "femgpu_adjoint_grad_device", "femgpu_solve_multi", "femgpu_solve_multi_device",
+    "femgpu_adjoint_grad_device", "femgpu_solve_multi", "femgpu_solve_multi_device", "femgpu_solve_batch",
     "femgpu_read_tetgen", "femgpu_read_ply", "femgpu_read_mat_sparse", "femgpu_read_mat_array",
     "femgpu_write_mat_array", "femgpu_write_vtk",
 ]
@@ -101,6 +101,8 @@ def lib():
     L.femgpu_adjoint_grad.argtypes = [_vp, _f64p, _f64p, _f64p, C.POINTER(SolveStats)]
     L.femgpu_solve_multi.argtypes = [_vp, C.c_int, _f64p, _f64p, C.POINTER(SolveStats)]
     L.femgpu_solve_multi_device.argtypes = [_vp, C.c_int, _vp, _i64, _vp, _i64, C.POINTER(SolveStats)]
+    L.femgpu_solve_batch.argtypes = [C.c_int, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), C.c_int, C.c_int,
+                                     C.POINTER(SolveStats)]
     L.femgpu_adjoint_grad_device.argtypes = [_vp, _vp, _vp, _vp, C.POINTER(SolveStats)]
     L.femgpu_get_matrix.argtypes = [_vp, _pi64, _pi64, _vp, _vp, _vp]
     L.femgpu_num_levels.argtypes = [_vp, C.POINTER(C.c_int)]
@@ -327,6 +329,25 @@ class Solver:
 
 
 # ---- file IO -----------------------------------------------------------------------------
+def solve_batch(solvers, bs, x0s=None, setup=True, threads=0, check=True):
+    """Independent problems at once (femgpu_solve_batch): solvers[i] (distinct handles,
+    each with its operator) solves bs[i]; returns the solutions and per-problem stats."""
+    k = len(solvers)
+    xs = [np.zeros(s.n) if x0s is None else np.array(x0s[i], dtype=np.float64) for i, s in enumerate(solvers)]
+    bs = [np.ascontiguousarray(b, dtype=np.float64) for b in bs]
+    hs = (_vp * k)(*[s.h for s in solvers])
+    pb = (_vp * k)(*[b.ctypes.data for b in bs])
+    px = (_vp * k)(*[x.ctypes.data for x in xs])
+    st = (SolveStats * k)()
+    status = lib().femgpu_solve_batch(k, hs, pb, px, 1 if setup else 0, threads, st)
+    if check and status != 0:
+        bad = next((s.h for s in solvers if lib().femgpu_last_error(s.h)), None)
+        _check(status, bad)
+    stats = [dict(iterations=t.iterations, relres=t.relative_residual, setup_ms=t.setup_ms, solve_ms=t.solve_ms,
+                  levels=t.num_levels) for t in st]
+    return xs, stats, status
+
+
 def read_tetgen(base: str):
     node, ele = (base + ".node").encode(), (base + ".ele").encode()
     nv, ne = C.c_int64(), C.c_int64()
