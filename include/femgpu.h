@@ -135,6 +135,15 @@ femgpu_status femgpu_set_matrix_csr(femgpu_handle h, int64_t n, const int32_t* r
  * (src/core/cuda/amg.cu:80-144) with createNextLevel / OldMIS / RAP. */
 femgpu_status femgpu_setup(femgpu_handle h);
 
+/* Writes the handle's AMG hierarchy (every level, the level-0 permutation and the outer
+ * operator) to a file, and reads one back into a handle that holds the same operator
+ * (checked by size and a fingerprint of its pattern and values; FEMGPU_ERR_INVALID
+ * otherwise) and the same precision setting, in place of femgpu_setup.  The file is in
+ * the writing machine's byte order.  No reference counterpart (the reference rebuilds
+ * its hierarchy in every AMG::setup). */
+femgpu_status femgpu_save_hierarchy(femgpu_handle h, const char* path);
+femgpu_status femgpu_load_hierarchy(femgpu_handle h, const char* path);
+
 /* Solves A x = b.  x holds the initial guess on entry (host arrays, n doubles).
  * solverType 0: one V-cycle; 1: PCG to tolerance.  Replaces FEMSolver::solveFEM
  * (src/FEMSolver.cu:58-93) -> AMG::solve (amg.cu:174-200) -> CG_Flex_Cycle

@@ -367,6 +367,16 @@ femgpu_status femgpu_setup(femgpu_handle h) {
   return guard(h, [&] { amg_setup(*h); });
 }
 
+femgpu_status femgpu_save_hierarchy(femgpu_handle h, const char* path) {
+  if (!h || !path) return FEMGPU_ERR_INVALID;
+  return guard(h, [&] { save_hierarchy(*h, path); });
+}
+
+femgpu_status femgpu_load_hierarchy(femgpu_handle h, const char* path) {
+  if (!h || !path) return FEMGPU_ERR_INVALID;
+  return guard(h, [&] { load_hierarchy(*h, path); });
+}
+
 femgpu_status femgpu_solve_device(femgpu_handle h, const double* d_b, double* d_x, femgpu_solve_stats* stats) {
   if (!h || !d_b || !d_x) return FEMGPU_ERR_INVALID;
   femgpu_status result = FEMGPU_OK;

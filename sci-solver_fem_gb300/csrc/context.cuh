@@ -178,6 +178,11 @@ void element_log_coef_gradient(Ctx& c, const double* d_lam, const double* d_u, d
 // amg_setup.cu
 void amg_setup(Ctx& c);
 
+// hierarchy_io.cu: the hierarchy to / from a file (the load checks that the handle holds
+// the operator it was built for)
+void save_hierarchy(Ctx& c, const char* path);
+void load_hierarchy(Ctx& c, const char* path);
+
 // amg_solve.cu
 struct SolveResult {
   int iterations = 0;

@@ -27,6 +27,7 @@ EXPORTS = [
     "femgpu_num_levels", "femgpu_get_level_info", "femgpu_level_get", "femgpu_vcycle", "femgpu_kernel_launches",
     "femgpu_profile_kernel", "femgpu_load_vector_device_noalloc", "femgpu_adjoint_grad",
     "femgpu_adjoint_grad_device", "femgpu_solve_multi", "femgpu_solve_multi_device", "femgpu_solve_batch",
+    "femgpu_save_hierarchy", "femgpu_load_hierarchy",
     "femgpu_read_tetgen", "femgpu_read_ply", "femgpu_read_mat_sparse", "femgpu_read_mat_array",
     "femgpu_write_mat_array", "femgpu_write_vtk",
 ]
@@ -101,6 +102,8 @@ def lib():
     L.femgpu_adjoint_grad.argtypes = [_vp, _f64p, _f64p, _f64p, C.POINTER(SolveStats)]
     L.femgpu_solve_multi.argtypes = [_vp, C.c_int, _f64p, _f64p, C.POINTER(SolveStats)]
     L.femgpu_solve_multi_device.argtypes = [_vp, C.c_int, _vp, _i64, _vp, _i64, C.POINTER(SolveStats)]
+    L.femgpu_save_hierarchy.argtypes = [_vp, C.c_char_p]
+    L.femgpu_load_hierarchy.argtypes = [_vp, C.c_char_p]
     L.femgpu_solve_batch.argtypes = [C.c_int, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), C.c_int, C.c_int,
                                      C.POINTER(SolveStats)]
     L.femgpu_adjoint_grad_device.argtypes = [_vp, _vp, _vp, _vp, C.POINTER(SolveStats)]
@@ -319,6 +322,17 @@ class Solver:
 
     def spmv_device(self, x_ptr: int, y_ptr: int):
         _check(lib().femgpu_spmv_device(self.h, _vp(x_ptr), _vp(y_ptr)), self.h)
+
+    def save_hierarchy(self, path: str):
+        """Writes the AMG hierarchy of the last setup to `path`."""
+        _check(lib().femgpu_save_hierarchy(self.h, os.fsencode(path)), self.h)
+
+    def load_hierarchy(self, path: str, check=True):
+        """Reads a hierarchy written for this same operator, in place of setup()."""
+        status = lib().femgpu_load_hierarchy(self.h, os.fsencode(path))
+        if check:
+            _check(status, self.h)
+        return status
 
     def load_vector_device_noalloc(self, f_ptr: int, b_ptr: int, check=True):
         """Device f -> device b on the handle's stream; allocates no device memory."""
