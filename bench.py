@@ -388,8 +388,8 @@ def main():
     t0 = time.perf_counter()
     for _ in range(args.steps):
         s.setup()
-        x_h[:] = 0.0
-        x_h, st2 = s.solve(b_h, x_h)
+        x_h[:] = 0.0  # the initial guess
+        x_h, st2 = s.solve(b_h, out=x_h)  # in place, as femgpu_solve
     e2e_ms = 1e3 * (time.perf_counter() - t0) / args.steps
     e2e = {"value": world * free / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": 16 * n,
            "d2h_bytes_per_step": 8 * n}

@@ -254,8 +254,17 @@ class Solver:
         _check(lib().femgpu_vcycle(self.h, np.ascontiguousarray(r, dtype=np.float64), z), self.h)
         return z
 
-    def solve(self, b, x0=None, check=True):
-        x = np.zeros(self.n) if x0 is None else np.array(x0, dtype=np.float64)
+    def solve(self, b, x0=None, check=True, out=None):
+        """Solves A x = b.  x0 is the initial guess (zeros when None); with `out` (a
+        contiguous float64 array of n entries holding the initial guess) the solve runs in
+        place there, as femgpu_solve does, instead of on a copy."""
+        if out is not None:
+            if not (isinstance(out, np.ndarray) and out.dtype == np.float64 and out.flags.c_contiguous
+                    and out.shape == (self.n,)):
+                raise ValueError("out must be a C-contiguous float64 array of the operator's size")
+            x = out
+        else:
+            x = np.zeros(self.n) if x0 is None else np.array(x0, dtype=np.float64)
         st = SolveStats()
         status = lib().femgpu_solve(self.h, np.ascontiguousarray(b, dtype=np.float64), x, C.byref(st))
         if check and status not in (0,):

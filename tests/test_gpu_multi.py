@@ -40,3 +40,19 @@ def test_multi_rhs_rejects_bad_leading_dimension():
     st = capi.SolveStats()
     # ldb smaller than the row count is refused before any device access
     assert capi.lib().femgpu_solve_multi_device(s.h, 1, C.c_void_p(16), 1, C.c_void_p(16), 1, C.byref(st)) == 1
+
+
+def test_in_place_solve_matches_copying_solve():
+    xyz, conn, kappa, f, mask = meshes.poisson3d_problem(10, sigma=2.0)
+    s = femgpu.Solver(solverType=1, tolerance=1e-8, maxIters=300, flexibleCG=1, seed=6)
+    s.set_mesh(xyz, conn)
+    s.assemble(kappa, 0.0)
+    s.set_dirichlet(mask)
+    b = np.where(mask.astype(bool), 0.0, s.load_vector(f))
+    s.setup()
+    x1, st1 = s.solve(b)
+    out = np.zeros(s.n)
+    x2, st2 = s.solve(b, out=out)
+    assert x2 is out and np.array_equal(x1, out) and st1["iterations"] == st2["iterations"]
+    with pytest.raises(ValueError):
+        s.solve(b, out=np.zeros(s.n, dtype=np.float32))
