@@ -368,10 +368,12 @@ int remove_small_parts(Ctx& c, int n, DBuf<int32_t>& part, const int32_t* weight
   return (int)removed;
 }
 
+// np: the number of partitions (labels 0 .. np-1, none empty) when the caller tracks it,
+// else -1 (then it is read from the labels).
 int restrict_partitions(Ctx& c, int max_size, int full_size, int n, const int32_t* xadj, const int32_t* adj,
-                        DBuf<int32_t>& part, const int32_t* w) {
+                        DBuf<int32_t>& part, const int32_t* w, int np = -1) {
   cudaStream_t s = c.stream;
-  int np = reduce_max(part.p, n, s) + 1;
+  if (np < 0) np = reduce_max(part.p, n, s) + 1;
   DBuf<int32_t> sizes(np, s), to(n, s);
   sizes.zero();
   FG_LAUNCH(histogram_kernel, grid_for(n, 256), 256, 0, s, n, part.p, w, sizes.p);
@@ -433,12 +435,14 @@ int aggregate(Ctx& c, int n, const int32_t* xadj, const int32_t* adj, int depth,
         if (removed == 0) return mis_count;
         mis_count -= removed;
       } else {
+        // the labels are still contiguous and non-empty here (the restriction below may
+        // empty a partition, but nothing reads the count after it): tracked, not read
         if (!first || mis_count < 10) {
-          restrict_partitions(c, max_size, full_size, n, xadj, adj, part, weights);
+          restrict_partitions(c, max_size, full_size, n, xadj, adj, part, weights, mis_count);
           return -1;
         }
         first = false;
-        remove_small_parts(c, n, part, weights, 1, 0, full_size, aggregated);
+        mis_count -= remove_small_parts(c, n, part, weights, 1, 0, full_size, aggregated, mis_count);
       }
     } else if (h[1] == 0) {
       // also the case where every aggregate was removed as undersized (the reference
