@@ -1931,11 +1931,6 @@ __global__ void partition_rows_kernel(int npart, const int32_t* part_idx, const 
   if (p < npart) rows[p] = agg_idx[part_idx[p + 1]] - agg_idx[part_idx[p]];
 }
 
-__global__ void row_lengths_kernel(int n, const int32_t* rp, int32_t* len) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) len[i] = rp[i + 1] - rp[i];
-}
-
 // In-partition entries per partition (the shared-memory footprint of the smoother).
 __global__ void partition_entries_kernel(int npart, const int32_t* part_idx, const int32_t* agg_idx,
                                          const int32_t* irp, int32_t* ent) {
