@@ -162,7 +162,8 @@ femgpu_status femgpu_solve_multi_device(femgpu_handle h, int nrhs, const double*
 
 /* Independent problems at once: for each i, femgpu_setup(h[i]) when setup != 0, then
  * femgpu_solve(h[i], b[i], x[i], &stats[i]) (host arrays, each the size of its own
- * operator).  The handles must be distinct, each with its own stream (the default);
+ * operator).  The handles must be distinct, each with its own stream (the default;
+ * handles sharing a stream are refused with FEMGPU_ERR_INVALID);
  * they run on up to `threads` host threads (0: one per handle), so the small problems'
  * setup round trips overlap and their kernels share the GPU.  Every problem is
  * attempted; the first failing status (in index order) is returned, and each failing

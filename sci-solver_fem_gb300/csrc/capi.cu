@@ -491,6 +491,11 @@ femgpu_status femgpu_solve_batch(int count, femgpu_handle* hs, const double* con
     if (!hs[i] || !b[i] || !x[i]) return FEMGPU_ERR_INVALID;
   std::sort(seen.begin(), seen.end());
   if (std::adjacent_find(seen.begin(), seen.end()) != seen.end()) return FEMGPU_ERR_INVALID;  // one thread per handle
+  // concurrent threads must not share a stream (each captures its PCG loop on its own)
+  std::vector<cudaStream_t> streams(count);
+  for (int i = 0; i < count; i++) streams[i] = hs[i]->stream;
+  std::sort(streams.begin(), streams.end());
+  if (std::adjacent_find(streams.begin(), streams.end()) != streams.end()) return FEMGPU_ERR_INVALID;
   std::vector<femgpu_status> status(count, FEMGPU_OK);
   std::atomic<int> next{0};
   auto work = [&]() {

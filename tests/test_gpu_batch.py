@@ -12,9 +12,9 @@ from femgpu import meshes
 pytestmark = pytest.mark.gpu
 
 
-def problem(n, seed):
+def problem(n, seed, **opts):
     xyz, conn, kappa, f, mask = meshes.poisson3d_problem(n, sigma=1.0, kappa_seed=seed, f_seed=1000 + seed)
-    s = femgpu.Solver(solverType=1, tolerance=1e-8, maxIters=300, flexibleCG=1, seed=1)
+    s = femgpu.Solver(solverType=1, tolerance=1e-8, maxIters=300, flexibleCG=1, seed=1, **opts)
     s.set_mesh(xyz, conn)
     s.assemble(kappa, 0.0)
     s.set_dirichlet(mask)
@@ -52,3 +52,12 @@ def test_batch_attempts_every_problem():
     good.setup()
     x1, _ = good.solve(b)
     assert np.array_equal(xs[1], x1)
+
+
+def test_batch_rejects_handles_on_one_stream():
+    torch = pytest.importorskip("torch")
+    stream = torch.cuda.Stream()
+    p1 = problem(3, 8, stream=stream.cuda_stream)
+    p2 = problem(4, 9, stream=stream.cuda_stream)
+    xs, stats, status = femgpu.solve_batch([p1[0], p2[0]], [p1[1], p2[1]], check=False)
+    assert status == 1  # FEMGPU_ERR_INVALID: their PCG captures would share the stream
