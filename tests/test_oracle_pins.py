@@ -125,3 +125,24 @@ def test_oracle_aggregation_invariants():
     assert np.array_equal(o["perm"], o2["perm"])
     o3 = O.oldmis(gx, ga, 90102, 512, seed=12)
     assert not np.array_equal(o["perm"], o3["perm"])
+
+
+def test_oracle_operator_symmetric_and_vcycle_homogeneous():
+    # the properties the full-size GPU test checks, on the oracle at a small size:
+    # the assembled operator (Dirichlet rows and columns eliminated) is exactly
+    # symmetric, and a V-cycle scales exactly with a power-of-two factor
+    xyz, conn, kappa, f, mask = meshes.poisson3d_problem(8, sigma=2.0)
+    rp, ci = O.build_pattern(xyz.shape[0], conn)
+    v = O.assemble(xyz, conn, rp, ci, coef=kappa, lambda_mass=0.0)
+    v, _ = O.apply_dirichlet(rp, ci, v, mask, None)
+    A = sp.csr_matrix((v, ci, rp))
+    D = (A - A.T).tocsr()
+    D.eliminate_zeros()
+    assert D.nnz == 0
+    gx, ga = meshes.adjacency_from_pattern(rp, ci)
+    for prec in (0, 1):
+        amg = O.OracleAMG(rp, ci, v, gx, ga, seed=2, fp64_hierarchy=prec)
+        r = np.random.default_rng(1).standard_normal(xyz.shape[0])
+        z = amg.vcycle(r)
+        assert np.array_equal(amg.vcycle(2.0 * r), 2.0 * z)
+        assert np.array_equal(amg.vcycle(0.25 * r), 0.25 * z)
