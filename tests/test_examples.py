@@ -44,3 +44,14 @@ def test_example_solves_reference_data(tmp_path, mesh, A, b, ans, bound, vtk):
     x_ans = matio.read(os.path.join(REF_DATA, ans))
     assert np.linalg.norm(x - x_ans) < bound
     assert (tmp_path / vtk).exists()
+
+
+def test_reference_test_programs_build(tmp_path):
+    # the reference's gtest programs restated against the drop-in (run by the GPU tests)
+    lib = capi.native_library_path()
+    exe = str(tmp_path / "reference_sanity")
+    src = os.path.join(ROOT, "tests", "cpp", "reference_sanity.cpp")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), src, lib, "-o", exe,
+                    f"-Wl,-rpath,{os.path.dirname(lib)}"], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode != 0  # no data directory given: usage, before any device call
