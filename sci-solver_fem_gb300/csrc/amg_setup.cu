@@ -8,9 +8,14 @@
 //   2. the permutation that makes aggregates and partitions contiguous;
 //   3. Ap = perm(A), the in/out-of-partition split used by the smoother;
 //   4. P = (I - omega D^-1 Ap) T, R = P^T;
-//   5. A_next = R (Ap P) by a row-wise expand-sort-compress SpGEMM in shared memory.
+//   5. A_next = R (Ap P), each product row accumulated in generation order by the
+//      tier its size calls for: a per-thread column list (large levels), a warp hash
+//      table, a block hash table or a dense accumulator;
+//   6. each parent's R rows and P columns put in the child's order, and the FP64 outer
+//      operator in level-0 order as 32-row slices.
 // Integer results are bit-identical to the CPU oracle for the same seed; floating
-// results use fixed summation orders (see row_esc_kernel).
+// results use fixed summation orders (generation order, ascending column), so they are
+// too.
 #include <algorithm>
 #include <chrono>
 #include <cstdio>

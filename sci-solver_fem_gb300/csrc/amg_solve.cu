@@ -1,17 +1,21 @@
 // amg_solve.cu -- V-cycle and FP64 outer PCG on the device.
 //
 // Smoother (gauss_seidel.cu, dsType 0 "symmetric" path): partition-block Jacobi.
-// One CTA per partition keeps the partition's x in shared memory and runs the
-// inner weighted-Jacobi sweeps over in-partition couplings; cross-partition
-// couplings enter once per relax (pre: preRRSym_kernel + preAout_kernel,
-// gauss_seidel.cu:1278-2015; post: postRelaxSym_kernel, :3626-3736).  In-partition
-// row sums run in a fixed lane order with fused multiply-adds (the reference
-// accumulates in shared-memory atomics in arbitrary order).
+// Consecutive partitions are packed into groups; a group's x lives in shared memory,
+// either of one persistent CTA with the entries in registers and the next group's
+// entries staged by bulk copies (level 0), or of a thread-block cluster whose CTAs
+// broadcast new values through distributed shared memory (coarse levels).  The inner
+// weighted-Jacobi sweeps run over in-partition couplings; cross-partition couplings
+// enter once per relax (pre: preRRSym_kernel + preAout_kernel, gauss_seidel.cu:1278-2015;
+// post: postRelaxSym_kernel, :3626-3736).  In-partition row sums run in a fixed lane
+// order with fused multiply-adds (the reference accumulates in shared-memory atomics in
+// arbitrary order).  Every non-coarsest level works in its own permuted order.
 //
 // PCG (CG_Flex_Cycle, cgcycle.cu:6-69) runs in FP64 on the level-0 permuted
 // numbering: b is permuted on entry and x back on exit, so the solved system is
-// A x = b (the reference applies the permuted operator to unpermuted vectors).
-// Reductions are two-stage with a fixed grid, so results are bitwise reproducible.
+// A x = b (the reference applies the permuted operator to unpermuted vectors).  The
+// whole loop is one CUDA graph with a device-side conditional.  Reductions are
+// two-stage with a fixed grid, so results are bitwise reproducible.
 #include <algorithm>
 #include <cmath>
 
