@@ -297,6 +297,8 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--cpu-sample", type=int, default=128,
                     help="cells per edge of the CPU oracle's problem (default: the full 128^3 workload)")
+    ap.add_argument("--cpu-sample-1t", type=int, default=48,
+                    help="cells per edge of the single-thread CPU sample (0: skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="poisson", choices=["poisson", "batched", "meshes", "differentiation"])
     args = ap.parse_args()
@@ -437,6 +439,11 @@ def main():
                "sample": f"{args.cpu_sample}^3-cell Kuhn mesh of the same problem ({(args.cpu_sample + 1) ** 3} "
                          f"vertices{', the full workload' if args.cpu_sample == args.n else ''}), oracle AMG setup + "
                          f"PCG to 1e-8, {dt:.1f} s"}
+        if args.cpu_sample_1t > 0:  # the same algorithm on one core, on a bounded sample
+            v1, dt1, _ = cpu_baseline(args.cpu_sample_1t, args.sigma, 1)
+            cpu["single_thread"] = {"value": v1, "unit": UNIT, "cores": 1,
+                                    "sample": f"{args.cpu_sample_1t}^3-cell Kuhn mesh of the same problem "
+                                              f"({(args.cpu_sample_1t + 1) ** 3} vertices), {dt1:.1f} s"}
 
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
