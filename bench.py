@@ -12,7 +12,8 @@ e2e = the same through femgpu_setup + femgpu_solve with host b/x buffers.
 --precision fp64: the same code with an FP64 hierarchy.
 --impl reference: the reference algorithm's CPU restatement (oracle) on host cores.
 --workload batched: 64^3 mesh with 64 seeded right-hand sides solved with one hierarchy
-  (femgpu_solve_multi); reports right-hand-side DOF/s.
+  (femgpu_solve_multi: eight columns at a time in lockstep PCGs with block kernels);
+  reports right-hand-side DOF/s, beside the same columns solved one at a time.
 --workload meshes: 48 independent cubes of 12^3..40^3 cells (seeded sizes), each with its own
   log-normal coefficient, set up and solved together through femgpu_solve_batch.
 --workload differentiation: 96^3 mesh, theta_e = log kappa_e ~ N(0,1), loss over a 1%
@@ -110,12 +111,20 @@ def cpu_problem(n_sample, sigma):
     return dict(rp=rp, ci=ci, v=v, b=b, gx=gx, ga=ga, free=int(xyz.shape[0] - mask.sum()))
 
 
-def cpu_baseline_run(prob, threads):
+def workload_config(n, sigma, dofs, free, elements, nnz, precision):
+    """The `config` of a bench line: the same for the GPU arm and the reference arm."""
+    return {"workload": f"poisson3d_kuhn_{n}^3_sigma{sigma:g}", "dofs": int(dofs), "free_dofs": int(free),
+            "elements": int(elements), "nnz": int(nnz), "precision": precision, "tolerance": 1e-8,
+            "l2": "inputs larger than L2 (A: %.0f MB)" % (12 * nnz / 1e6)}
+
+
+def cpu_baseline_run(prob, threads, fp64=False):
     """The reference algorithm restated on the CPU (oracle), timed on host cores:
     AMG setup + flexible PCG to 1e-8 on a prebuilt problem."""
     import oracle as O
     t0 = time.perf_counter()
-    amg = O.OracleAMG(prob["rp"], prob["ci"], prob["v"], prob["gx"], prob["ga"], seed=1, threads=threads)
+    amg = O.OracleAMG(prob["rp"], prob["ci"], prob["v"], prob["gx"], prob["ga"], seed=1, threads=threads,
+                      fp64_hierarchy=1 if fp64 else 0)
     x, st = amg.pcg(prob["b"], tol=1e-8, max_iters=500, flexible=True)
     dt = time.perf_counter() - t0
     return prob["free"] / dt, dt, st
@@ -153,11 +162,27 @@ def run_batched(args):
             times.append(time.perf_counter() - t0)
             iters.append(st["iterations"])
     dt = float(np.mean(times))
+    # the same 64 columns one at a time (single-column solves on the same hierarchy)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s.setup()
+    it1 = 0
+    for j in range(k):
+        dX[j].zero_()
+        it1 += s.solve_device(dB[j].data_ptr(), dX[j].data_ptr())["iterations"]
+    torch.cuda.synchronize()
+    dt1 = time.perf_counter() - t0
+    rp, ci, _ = s.matrix()
     out = {"metric": "batched AMG-PCG right-hand-side DOF/s (64 RHS, one hierarchy)", "value": k * free / dt,
            "unit": "DOF*RHS/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt,
            "higher_is_better": True, "dtype": "f64+f32", "data": "synthetic",
-           "config": {"workload": "poisson3d_kuhn_64^3_64rhs", "dofs": n, "free_dofs": free, "nrhs": k},
-           "pcg_iterations_total": int(np.mean(iters)), "relres_max": st["relres"]}
+           "config": {"workload": "poisson3d_kuhn_64^3_64rhs", "dofs": n, "free_dofs": free, "nrhs": k,
+                      "block": 8},
+           "pcg_iterations_total": int(np.mean(iters)), "relres_max": st["relres"],
+           "outer_operator_reads_per_rhs_iteration": 1.0 / 8.0,
+           "outer_operator_bytes_per_rhs_iteration": 12.0 * ci.shape[0] / 8.0,
+           "single_column_solves_ms": 1e3 * dt1, "single_column_iterations_total": it1,
+           "speedup_vs_single_column_solves": dt1 / dt}
     print(json.dumps(out))
 
 
@@ -203,10 +228,12 @@ def run_meshes(args):
 
 
 def run_differentiation(args):
-    """96^3 mesh: forward solve + adjoint gradient per step; gradient vs an FP64 one."""
+    """96^3 mesh: forward solve + adjoint gradient per step (mixed precision, PCG to 1e-10);
+    the gradient is compared with the FP64-hierarchy gradient solved to 1e-12 and with
+    central differences (h = 1e-6) on 32 seeded elements."""
     import torch
     import femgpu
-    from femgpu import meshes
+    from femgpu import gradcheck, meshes
     xyz, conn = meshes.kuhn_cube(96)
     n, ne = xyz.shape[0], conn.shape[0]
     mask = (xyz[:, 2] == 0.0).astype(np.uint8)
@@ -215,23 +242,25 @@ def run_differentiation(args):
     S = np.random.default_rng(10).choice(n, n // 100, replace=False)
     theta_obs = np.random.default_rng(11).standard_normal(ne)
     f = np.random.default_rng(5).uniform(-1.0, 1.0, n)
+    tol = 1e-10
 
     def forward(th, precision, tol):
-        s = femgpu.Solver(solverType=1, tolerance=tol, maxIters=2000, flexibleCG=1, seed=1, precision=precision)
+        s = femgpu.Solver(solverType=1, tolerance=tol, maxIters=3000, flexibleCG=1, seed=1, precision=precision)
         s.set_mesh(xyz, conn)
         b = np.where(mask.astype(bool), 0.0, s.load_vector(f))
         s.assemble(np.exp(th), 0.0)
         s.set_dirichlet(mask)
         s.setup()
         u, st = s.solve(b)
-        return s, u
+        return s, u, b
 
-    _, u_obs = forward(theta_obs, 1, 1e-12)
+    s_obs, u_obs, _ = forward(theta_obs, 1, 1e-12)
+    s_obs.close()
     times, fwd_ms, adj_ms = [], [], []
     for step in range(args.warmup + args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        s, u = forward(theta, 0, 1e-8)
+        s, u, b = forward(theta, 0, tol)
         t1 = time.perf_counter()
         r = np.zeros(n)
         r[S] = u[S] - u_obs[S]
@@ -243,17 +272,28 @@ def run_differentiation(args):
             adj_ms.append(1e3 * (t2 - t1))
         s.close()
     # FP64 hierarchy, 1e-12 forward and adjoint: the reference gradient
-    sr, ur = forward(theta, 1, 1e-12)
+    sr, ur, _ = forward(theta, 1, 1e-12)
     rr = np.zeros(n)
     rr[S] = ur[S] - u_obs[S]
     gr, _ = sr.adjoint_grad(rr, ur)
+    sr.close()
     rel = float(np.linalg.norm(g - gr) / np.linalg.norm(gr))
+    elems = np.random.default_rng(12).choice(ne, 32, replace=False)
+    t_fd = time.perf_counter()
+    fd = gradcheck.central_differences(xyz, conn, theta, mask, b, S, u_obs, elems, h=1e-6)
+    t_fd = time.perf_counter() - t_fd
+    fd_rel = float(np.linalg.norm(fd - g[elems]) / np.linalg.norm(fd))
     out = {"metric": "forward + adjoint gradient wall time (96^3, mixed precision)",
            "value": 1e3 * float(np.mean(times)), "unit": "ms", "higher_is_better": False, "n_gpus": 1,
            "steps": args.steps, "warmup": args.warmup, "data": "synthetic",
-           "config": {"workload": "poisson3d_kuhn_96^3_adjoint", "dofs": n, "elements": ne, "observed": len(S)},
+           "config": {"workload": "poisson3d_kuhn_96^3_adjoint", "dofs": n, "elements": ne, "observed": len(S),
+                      "tolerance": tol},
            "forward_ms": float(np.mean(fwd_ms)), "adjoint_ms": float(np.mean(adj_ms)),
-           "gradient_rel_error_vs_fp64_1e-12": rel}
+           "gradient_rel_error_vs_fp64_1e-12": rel,
+           "central_differences": {"elements": len(elems), "h": 1e-6, "rel_error_vs_adjoint": fd_rel,
+                                   "seconds": round(t_fd, 1),
+                                   "how": "(L(theta+h) - L(theta-h)) / 2h with u+ - u- = -A+^-1 (A+ - A-) u-, "
+                                          "FP64-hierarchy solves to 1e-12"}}
     print(json.dumps(out))
 
 
@@ -265,22 +305,26 @@ def run_reference(args):
     threads = len(os.sched_getaffinity(0))
     n_sample = args.cpu_sample
     prob = cpu_problem(n_sample, args.sigma)
+    fp64 = args.precision == "fp64"
     for _ in range(args.warmup):
-        cpu_baseline_run(prob, threads)
+        cpu_baseline_run(prob, threads, fp64)
     vals, times = [], []
     for _ in range(args.steps):
-        v, dt, st = cpu_baseline_run(prob, threads)
+        v, dt, st = cpu_baseline_run(prob, threads, fp64)
         vals.append(v)
         times.append(dt)
     value = float(np.mean(vals))
     what = "the full workload" if n_sample == args.n else "a sample of the same Poisson problem family"
     sample = (f"{n_sample}^3-cell Kuhn tet mesh, {what} ({(n_sample + 1) ** 3} vertices), "
-              f"AMG setup + PCG to 1e-8 per step")
+              f"AMG setup + PCG to 1e-8 per step, {threads} threads")
+    ne = 6 * n_sample ** 3
     out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(times)),
-           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-           "data": "synthetic", "config": {"workload": f"poisson3d_kuhn_{args.n}^3_sigma{args.sigma:g}",
-                                           "parallelism": "host cores"},
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64+f32" if args.precision == "mixed" else "f64", "data": "synthetic",
+           "config": workload_config(n_sample, args.sigma, prob["rp"].shape[0] - 1, prob["free"], ne,
+                                     int(prob["ci"].shape[0]), args.precision),
+           "execution": f"CPU oracle (the reference algorithm restated), {threads} host threads",
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
@@ -397,29 +441,66 @@ def main():
            "d2h_bytes_per_step": 8 * n}
     clk = clocks.stop()
 
-    # ---- rooflines: each hot kernel of a PCG iteration timed with CUDA events on the
-    # solver's stream by the library (femgpu_profile_kernel); each runs once per
-    # iteration, so the dominant one has the largest time per launch
+    # ---- the same workload with the FP64 hierarchy (the metric's "mixed vs FP64" half):
+    # same problem, same stream, same timing; one solver per precision
+    s64 = femgpu.Solver(solverType=1, tolerance=1e-8, maxIters=500, flexibleCG=1, seed=1, precision=1,
+                        device=local, stream=stream.cuda_stream)
+    s64.set_mesh(xyz, conn)
+    s64.assemble(kappa, 0.0)
+    s64.set_dirichlet(mask)
+    d_x64 = torch.zeros(n, dtype=torch.float64, device="cuda")
+
+    def step64():
+        s64.setup()
+        d_x64.zero_()
+        return s64.solve_device(d_b.data_ptr(), d_x64.data_ptr())
+
+    for _ in range(args.warmup):
+        step64()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    st64s = [step64() for _ in range(args.steps)]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms64 = e0.elapsed_time(e1) / args.steps
+    fp64 = {"ms_per_step": ms64, "value": world * free / (ms64 / 1e3), "unit": UNIT,
+            "setup_ms": float(np.mean([t["setup_ms"] for t in st64s])),
+            "solve_ms": float(np.mean([t["solve_ms"] for t in st64s])),
+            "pcg_iterations": st64s[-1]["iterations"], "relres": st64s[-1]["relres"]}
+    s64.close()
+
+    # ---- rooflines: each hot kernel timed with CUDA events on the solver's stream by the
+    # library (femgpu_profile_kernel).  The V-cycle's level-0 post-smoother is timed as a
+    # PCG iteration runs it (selector 5); the dominant kernel has the largest time per
+    # launch among those that run once per PCG iteration.
     peak, peak_kind = peaks()
     rp, ci, _ = s.matrix()
     nnz = int(ci.shape[0])
-    traffic = {}
-    tpath = os.path.join(ROOT, "profiles", "dram_traffic_128cube.json")
+    cfg = workload_config(args.n, args.sigma, n, free, conn.shape[0], nnz, args.precision)
+    traffic, traffic_cmd = {}, None
+    tpath = os.path.join(ROOT, "profiles", "dram_traffic.json")
     if os.path.exists(tpath):
         with open(tpath) as fh:
-            traffic = json.load(fh)
+            tr = json.load(fh)
+        # measured DRAM bytes per launch apply only to the configuration they were taken on
+        key = f"{cfg['workload']}_{args.precision}"
+        traffic = tr.get("per_launch", {}).get(key, {})
+        traffic_cmd = tr.get("commands", {}).get(key)
     rooflines = []
-    for which, name in femgpu.Solver.KERNELS.items():
+    for which in (0, 1, 5, 3, 4, 6, 7):
+        name = femgpu.Solver.KERNELS[which]
         kms, kbytes = s.profile_kernel(which, reps=20)
         ach = kbytes / (kms / 1e3) / 1e9
         entry = {"bound": "hbm", "kernel": name, "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                  "frac": round(ach / peak, 4), "traffic": traffic.get(name), "peak_source": peak_kind,
-                 "algorithmic_bytes": kbytes, "ms": round(kms, 4)}
-        fp64 = traffic.get("_fp64_pipe_active", {}).get(name)
-        if fp64 is not None:  # ncu sm__pipe_fp64_cycles_active of the same kernel (GB300: 2 DFMA/clk/SM)
-            entry["fp64_pipe_active"] = fp64
+                 "algorithmic_bytes": kbytes, "ms": round(kms, 4),
+                 "per": "assembly" if which >= 6 else "PCG iteration"}
+        fp64_pipe = traffic.get("_fp64_pipe_active", {}).get(name)
+        if fp64_pipe is not None:  # ncu sm__pipe_fp64_cycles_active of the same kernel
+            entry["fp64_pipe_active"] = fp64_pipe
         rooflines.append(entry)
-    roofline = max(rooflines, key=lambda r: r["ms"])
+    roofline = max((r for r in rooflines if r["per"] == "PCG iteration"), key=lambda r: r["ms"])
+    assembly_device_ms = sum(r["ms"] for r in rooflines if r["per"] == "assembly")
 
     # final error of the timed solve against an FP64-hierarchy PCG solved to 1e-12
     x_mixed = d_x.cpu().numpy()
@@ -449,16 +530,14 @@ def main():
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f64+f32" if prec == 0 else "f64", "data": "synthetic",
-               "config": {"workload": f"poisson3d_kuhn_{args.n}^3_sigma{args.sigma:g}", "dofs": n,
-                          "free_dofs": free, "elements": int(conn.shape[0]), "nnz": nnz,
-                          "precision": args.precision, "tolerance": 1e-8, "parallelism": "replicas" if world > 1 else "1 GPU",
-                          "l2": "inputs larger than L2 (A: %.0f MB)" % (12 * nnz / 1e6)},
+               "config": cfg, "execution": "replicas" if world > 1 else "1 GPU",
                "pcg_iterations": iters[-1], "relres": relres, "setup_ms": float(np.mean(setup_ms)),
                "solve_ms": float(np.mean(solve_ms)), "assembly_ms": assembly_ms,
+               "assembly_device_ms": assembly_device_ms,
+               "fp64_hierarchy": fp64, "mixed_speedup_vs_fp64": fp64["ms_per_step"] / ms if prec == 0 else None,
                "error_vs_fp64_1e-12": final_error, "fp64_1e-12_iterations": st_ref["iterations"],
                "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "rooflines": rooflines,
-               "cpu_baseline": cpu,
-               "clocks": clk}
+               "traffic_source": traffic_cmd, "cpu_baseline": cpu, "clocks": clk}
         print(json.dumps(out))
     if dist:
         dist.destroy_process_group()

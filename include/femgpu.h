@@ -151,9 +151,14 @@ femgpu_status femgpu_load_hierarchy(femgpu_handle h, const char* path);
 femgpu_status femgpu_solve(femgpu_handle h, const double* b, double* x, femgpu_solve_stats* stats);
 
 /* nrhs right-hand sides with one hierarchy: column j of B (and of X, which holds the
- * initial guesses) is nverts doubles at B + j * nverts (host arrays).  stats: summed
- * iterations, largest relative residual, total solve time.  No reference counterpart
- * (the reference solves one right-hand side per FEMSolver::solveFEM). */
+ * initial guesses) is nverts doubles at B + j * nverts (host arrays).  With solverType 1
+ * the columns are solved eight at a time: each column runs its own flexible PCG, the
+ * eight in lockstep, and every operator and V-cycle application works on the n x 8 block
+ * at once (sparse matrix times block), so the operators are read once per eight columns;
+ * a column stops when it reaches the tolerance.  stats: summed iterations, largest
+ * relative residual, total solve time; the first failing column's status is returned.
+ * No reference counterpart (the reference solves one right-hand side per
+ * FEMSolver::solveFEM). */
 femgpu_status femgpu_solve_multi(femgpu_handle h, int nrhs, const double* B, double* X,
                                  femgpu_solve_stats* stats);
 /* Same with device arrays and leading dimensions ldb, ldx >= nverts. */
@@ -203,14 +208,17 @@ femgpu_status femgpu_spmv_device(femgpu_handle h, const double* d_x, double* d_y
  * cap, where a hidden allocation mid-step can fail.
  * The two per-element scratch arrays live in a fixed region built into the
  * library: 2 x FEMGPU_NOALLOC_MAX_ELEMENTS doubles (32 MiB) per device, reserved
- * when this part of the library is first used.  Meshes with more elements are
+ * when this part of the library is first used under CUDA's lazy module loading (the
+ * default since CUDA 12.2; with CUDA_MODULE_LOADING=EAGER, when the library is
+ * loaded into a device context).  Meshes with more elements are
  * rejected with FEMGPU_ERR_LIMIT.  Nothing in the region has to start at zero:
  * each call writes every slot it reads.
  * The region is shared by every handle on a device, so calls that can overlap
  * on one device (different streams or threads) race; calls on one stream are
  * ordered.  The work is enqueued on the handle's stream and the call returns
- * without waiting.  The first call on each device looks the region up (and may
- * load this part of the library): make it before any stream capture begins. */
+ * without waiting.  The first call on each handle looks the region up (the first
+ * on a device may also load this part of the library): make it before any stream
+ * capture begins. */
 #define FEMGPU_NOALLOC_MAX_ELEMENTS 2097152
 femgpu_status femgpu_load_vector_device_noalloc(femgpu_handle h, const double* d_f, double* d_b);
 
@@ -230,12 +238,21 @@ femgpu_status femgpu_level_get(femgpu_handle h, int level, int32_t* A_rowptr, in
                                int32_t* P_rowptr, int32_t* P_cols, double* P_vals);
 /* One V-cycle z = M r on host vectors (AMG_Level::cycle_level0, amg_level.cu:74-128). */
 femgpu_status femgpu_vcycle(femgpu_handle h, const double* r, double* z);
-/* Times one hot kernel of the current hierarchy with CUDA events on the handle's
- * stream (3 untimed launches, then `reps`) and reports its average time and its
- * algorithmic bytes per launch: 0 = outer PCG FP64 SpMV (+ dot), 1 = level-0
- * pre-smoother, 2 = level-0 post-smoother relax, 3 = level-0 restriction,
- * 4 = level-0 prolongation.  No reference counterpart (measurement support). */
+/* Times one hot kernel with CUDA events on the handle's stream (3 untimed launches,
+ * then `reps`) and reports its average time and its algorithmic bytes per launch:
+ * 0 = outer PCG FP64 SpMV (+ dot), 1 = level-0 pre-smoother, 2 = level-0 post-smoother
+ * sweeps alone, 3 = level-0 restriction, 4 = level-0 prolongation, 5 = the level-0
+ * post-smoother as a PCG iteration runs it (b - A_out x, sweeps, z in FP64 and the z.r
+ * partials), 6 = the assembly's element kernel, 7 = its row-gather kernel (6 and 7 need
+ * an operator assembled from the mesh, 0-5 a hierarchy; the operator is not changed).
+ * No reference counterpart (measurement support). */
 femgpu_status femgpu_profile_kernel(femgpu_handle h, int which, int reps, double* avg_ms, double* bytes);
+/* Failure-detection testing: the level-0 register smoother waits at most `polls` polls
+ * for the bulk copies of each group's entries before it records FEMGPU_ERR_LIMIT for the
+ * solve (0: it gives up at once; negative: the default limit again).  A smoother CTA that
+ * gives up still waits, with the full limit, for the copies it started, so the context
+ * stays usable.  No reference counterpart. */
+femgpu_status femgpu_test_copy_wait_limit(femgpu_handle h, int polls);
 /* Number of kernel launches issued by the library on this handle so far. */
 femgpu_status femgpu_kernel_launches(femgpu_handle h, int64_t* count);
 

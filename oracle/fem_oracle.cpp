@@ -309,6 +309,54 @@ void element3d(const double x[4], const double y[4], const double z[4], double c
     }
 }
 
+/* Element 3D in the library's fused multiply-add formulation (fem_assembly.cu
+ * tet_gradients / element3d_kernel, restated operation for operation): edge vectors
+ * a = p1 - p0, b = p2 - p0, c = p3 - p0, det = a . (b x c), grad l1..3 = (b x c, c x a,
+ * a x b) / det, grad l0 = -((grad l1 + grad l2) + grad l3), K_ab = (|det| / 6) co grad
+ * l_a . grad l_b, mass integrand * |det| / 8.  It agrees with element3d (the
+ * reference's cofactor inverse) to a few units in the last place. */
+static void cross_fma(const double u[3], const double v[3], double w[3]) {
+  w[0] = std::fma(u[1], v[2], -(u[2] * v[1]));
+  w[1] = std::fma(u[2], v[0], -(u[0] * v[2]));
+  w[2] = std::fma(u[0], v[1], -(u[1] * v[0]));
+}
+
+void element3d_fma(const double x[4], const double y[4], const double z[4], double co, double lambda,
+                   const double integrand[10], double out[10]) {
+  double p[4][3];
+  for (int q = 0; q < 4; q++) {
+    p[q][0] = x[q];
+    p[q][1] = y[q];
+    p[q][2] = z[q];
+  }
+  double a[3], b[3], c[3], bc[3], ca[3], ab[3], g[4][3];
+  for (int d = 0; d < 3; d++) {
+    a[d] = p[1][d] - p[0][d];
+    b[d] = p[2][d] - p[0][d];
+    c[d] = p[3][d] - p[0][d];
+  }
+  cross_fma(b, c, bc);
+  cross_fma(c, a, ca);
+  cross_fma(a, b, ab);
+  const double det = std::fma(a[0], bc[0], std::fma(a[1], bc[1], a[2] * bc[2]));
+  const double inv = 1.0 / det;
+  for (int d = 0; d < 3; d++) {
+    g[1][d] = bc[d] * inv;
+    g[2][d] = ca[d] * inv;
+    g[3][d] = ab[d] * inv;
+    g[0][d] = -((g[1][d] + g[2][d]) + g[3][d]);
+  }
+  const double wk = (fabs(det) / 6.0) * co;
+  const double jac = fabs(det) * 0.125;
+  int cnt = 0;
+  for (int k = 0; k < 4; k++)
+    for (int q = k; q < 4; q++) {
+      const double st = std::fma(g[k][0], g[q][0], std::fma(g[k][1], g[q][1], g[k][2] * g[q][2])) * wk;
+      out[cnt] = std::fma(lambda, integrand[cnt] * jac, st);
+      cnt++;
+    }
+}
+
 /* Element 2D (perform_element_loop_2D.cuh:29-147,287-372): 6 upper entries
  * (0,0),(0,1),(0,2),(1,1),(1,2),(2,2). */
 void element2d(const double x[3], const double y[3], double co, double lambda, const double zx[6],
@@ -1491,7 +1539,8 @@ int64_t orc_build_pattern(int nv, int ne, int nvpe, const int32_t* conn, int32_t
 }
 
 int orc_assemble(int dim, int nv, const double* xyz, int ne, const int32_t* conn, const int32_t* labels,
-                 const double* coef, double lambda_mass, const int32_t* rowptr, const int32_t* cols, double* vals) {
+                 const double* coef, double lambda_mass, const int32_t* rowptr, const int32_t* cols, double* vals,
+                 int reference_formula) {
   int64_t nnz = rowptr[nv];
   std::fill(vals, vals + nnz, 0.0);
   if (dim == 3) {
@@ -1508,7 +1557,8 @@ int orc_assemble(int dim, int nv, const double* xyz, int ne, const int32_t* conn
       }
       double co = coef ? coef[e] : (labels ? label_coefficient(labels[e]) : 1.0);
       double ev[10];
-      element3d(x, y, z, co, lambda_mass, integ, ev);
+      if (reference_formula) element3d(x, y, z, co, lambda_mass, integ, ev);
+      else element3d_fma(x, y, z, co, lambda_mass, integ, ev);
       for (int q = 0; q < 10; q++) {
         int i = id[pr[q][0]], j = id[pr[q][1]];
         int64_t s = find_col(rowptr, cols, i, j);

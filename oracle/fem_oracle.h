@@ -43,10 +43,14 @@ int64_t orc_build_pattern(int nv, int ne, int nvpe, const int32_t* conn,
  * dim 2: triangles (perform_element_loop_2D.cuh:287-372).  xyz holds 3 doubles per
  * vertex in both cases (z ignored in 2D).  coef[e] scales element e's stiffness; when
  * coef is NULL the 3D coefficient comes from labels (co table) and 2D uses 1.
- * vals receives A = sum_e coef_e K_e + lambda_mass M_e, summed in element order. */
+ * vals receives A = sum_e coef_e K_e + lambda_mass M_e, summed in element order.
+ * Tetrahedra: reference_formula = 1 evaluates the reference's 4x4 cofactor inverse term
+ * for term (perform_element_loop_3D.cuh:525-583); 0 evaluates the library's fused
+ * multiply-add gradients (fem_assembly.cu tet_gradients), which the GPU matches bit for
+ * bit and which agree with the reference formula to 1e-13 relative. */
 int orc_assemble(int dim, int nv, const double* xyz, int ne, const int32_t* conn,
                  const int32_t* labels, const double* coef, double lambda_mass,
-                 const int32_t* rowptr, const int32_t* cols, double* vals);
+                 const int32_t* rowptr, const int32_t* cols, double* vals, int reference_formula);
 
 /* Consistent P1 load vector b_i = sum_e int f_h phi_i (exact P1 mass). */
 int orc_load_vector(int dim, int nv, const double* xyz, int ne, const int32_t* conn,

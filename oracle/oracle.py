@@ -48,7 +48,7 @@ def lib():
         L.orc_build_pattern.argtypes = [C.c_int, C.c_int, C.c_int, _i32p, _i32p, _i32p, C.c_int64]
         L.orc_build_pattern.restype = C.c_int64
         L.orc_assemble.argtypes = [C.c_int, C.c_int, _f64p, C.c_int, _i32p, C.c_void_p, C.c_void_p,
-                                   C.c_double, _i32p, _i32p, _f64p]
+                                   C.c_double, _i32p, _i32p, _f64p, C.c_int]
         L.orc_load_vector.argtypes = [C.c_int, C.c_int, _f64p, C.c_int, _i32p, _f64p, _f64p]
         L.orc_apply_dirichlet.argtypes = [C.c_int, _i32p, _i32p, _f64p, _u8p, C.c_void_p]
         L.orc_random_mis.argtypes = [C.c_int, _i32p, _i32p, C.c_int, C.c_uint32, _i32p]
@@ -105,7 +105,10 @@ def build_pattern(nv: int, conn: np.ndarray):
     return rowptr, cols[:nnz].copy()
 
 
-def assemble(xyz, conn, rowptr, cols, labels=None, coef=None, lambda_mass=1.0):
+def assemble(xyz, conn, rowptr, cols, labels=None, coef=None, lambda_mass=1.0, reference_formula=False):
+    """A = sum_e coef_e K_e + lambda_mass M_e on the pattern.  Tetrahedra: the library's
+    fused multiply-add gradients by default (what the GPU computes, bit for bit); with
+    reference_formula the reference's 4x4 cofactor inverse."""
     conn = np.ascontiguousarray(conn, dtype=np.int32)
     dim = 3 if conn.shape[1] == 4 else 2
     xyz = np.ascontiguousarray(xyz, dtype=np.float64)
@@ -113,7 +116,7 @@ def assemble(xyz, conn, rowptr, cols, labels=None, coef=None, lambda_mass=1.0):
     coef = None if coef is None else np.ascontiguousarray(coef, dtype=np.float64)
     vals = np.zeros(cols.shape[0])
     st = lib().orc_assemble(dim, xyz.shape[0], xyz.ravel(), conn.shape[0], conn.ravel(), _ptr(labels),
-                            _ptr(coef), float(lambda_mass), rowptr, cols, vals)
+                            _ptr(coef), float(lambda_mass), rowptr, cols, vals, int(bool(reference_formula)))
     if st:
         raise ValueError("assembly failed")
     return vals

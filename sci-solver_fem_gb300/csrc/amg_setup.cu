@@ -1954,11 +1954,74 @@ __global__ void partition_starts_kernel(int npart, const int32_t* part_idx, cons
   }
 }
 
-// In-partition columns relative to the first row of their group (one CTA per group).
-__global__ void group_local_cols_kernel(const int32_t* grows, const int32_t* irp, const int32_t* ici,
-                                        uint16_t* c16) {
+// The register smoother's entry layout, one CTA of 512 threads per group, warp w taking
+// the group's rows [rs + 32w, rs + 32w + 32) (a block):
+// * the block's rows are ranked by decreasing in-partition length (ties: lower row
+//   first); jrow[block start + p] = offset in the block of the row ranked p;
+// * entry k of the row ranked p goes to (block's first entry) + m_0 + ... + m_{k-1} + p,
+//   m_j = rows of the block longer than j (a jagged-diagonal layout of the block);
+// * each entry's column becomes (column - rs) + c * xcopy_stride<T>(): the copy c of x
+//   is chosen greedily per diagonal, entries in lane order, each distinct column taking
+//   the copy whose shared-memory bank has held the fewest distinct columns of that
+//   diagonal so far (ties: the lowest copy); equal columns share the first one's copy.
+// Entry values and the order of each row's entries are unchanged: only where they sit.
+template <class T>
+__global__ void __launch_bounds__(512) jds_build_kernel(const int32_t* __restrict__ grows,
+                                                        const int32_t* __restrict__ irp,
+                                                        const int32_t* __restrict__ ici, const T* __restrict__ iv,
+                                                        T* __restrict__ jv, uint16_t* __restrict__ jc,
+                                                        uint8_t* __restrict__ jrow) {
+  constexpr unsigned kAll = 0xffffffffu;
+  constexpr int CS = xcopy_stride<T>();
+  constexpr int NB = sizeof(T) == 4 ? 32 : 16;  // bank slots of one element size
+  constexpr int SHIFT = NB / kXCopies;          // bank slots between copies
   const int rs = grows[blockIdx.x], re = grows[blockIdx.x + 1];
-  for (int q = irp[rs] + threadIdx.x; q < irp[re]; q += blockDim.x) c16[q] = (uint16_t)(ici[q] - rs);
+  const int lane = threadIdx.x & 31;
+  const int r0 = rs + (threadIdx.x & ~31);
+  if (r0 >= re) return;  // the whole warp: its block is empty
+  const int row = r0 + lane;
+  const bool live = row < re;
+  const int len = live ? irp[row + 1] - irp[row] : 0;
+  const unsigned key = live ? ((unsigned)(len + 1) << 5) | (unsigned)(31 - lane) : 0u;
+  int rank = 0;
+  for (int j = 0; j < 32; j++) rank += __shfl_sync(kAll, key, j) > key;
+  if (live) jrow[r0 + rank] = (uint8_t)lane;
+  const int eb = irp[r0];
+  const int mine = live ? irp[row] : 0;
+  int dk = 0;  // entries on the diagonals before k
+  for (int k = 0;; k++) {
+    const bool act = k < len;
+    const unsigned am = __ballot_sync(kAll, act);
+    if (!am) break;
+    const int a = act ? ici[mine + k] - rs : -1;
+    const unsigned same = __match_any_sync(kAll, a);
+    const int leader = __ffs(same) - 1;
+    unsigned todo = __ballot_sync(kAll, act && leader == lane);
+    int load = 0;  // lane b: distinct columns of this diagonal placed in bank slot b
+    int copy = 0;
+    while (todo) {
+      const int q = __ffs(todo) - 1;
+      todo &= todo - 1;
+      const int aq = __shfl_sync(kAll, a, q);
+      int best = 0, bc = 0;
+      for (int c = 0; c < kXCopies; c++) {
+        const int lb = __shfl_sync(kAll, load, (aq + c * SHIFT) % NB);
+        if (c == 0 || lb < best) {
+          best = lb;
+          bc = c;
+        }
+      }
+      if (lane == (aq + bc * SHIFT) % NB) load++;
+      if (lane == q) copy = bc;
+    }
+    copy = __shfl_sync(kAll, copy, leader);
+    if (act) {
+      const int dst = eb + dk + rank;
+      jv[dst] = iv[mine + k];
+      jc[dst] = (uint16_t)(a + copy * CS);
+    }
+    dk += __popc(am);
+  }
 }
 
 // Smoother work groups: consecutive partitions packed greedily into one CTA while
@@ -2141,10 +2204,14 @@ void build_levels(Ctx& c, Hierarchy<T>& H) {
       pt.mark("split rows");
       if (smoother_in_registers(L.max_in_row, L.max_part_rows)) {
         build_smoother_groups(c, L, kRegGroupRows, std::numeric_limits<int>::max());
-        L.ci16.alloc(L.Ain.nnz + 16, s);
-        L.ci16.zero();
+        L.jv.alloc(L.Ain.nnz + 16, s);
+        L.jv.zero();
+        L.jc16.alloc(L.Ain.nnz + 16, s);
+        L.jc16.zero();
+        L.jrow.alloc(N, s);
         if (L.ngroups > 0)
-          FG_LAUNCH(group_local_cols_kernel, L.ngroups, 256, 0, s, L.grows.p, L.Ain.rp.p, L.Ain.ci.p, L.ci16.p);
+          FG_LAUNCH(jds_build_kernel<T>, L.ngroups, kRegGroupRows, 0, s, L.grows.p, L.Ain.rp.p, L.Ain.ci.p,
+                    L.Ain.v.p, L.jv.p, L.jc16.p, L.jrow.p);
       } else
         build_smoother_groups(c, L, L.max_part_rows, L.max_part_entries);
       pt.mark("groups");

@@ -333,9 +333,9 @@ __device__ __forceinline__ T gather_row(const int32_t* __restrict__ ci, const T*
   return s;
 }
 
-// Shared memory of the register smoother: two mbarriers, x twice (kRegGroupRows + 1
-// slots each; the last slot stays 0 for padded entries), then two staging buffers for
-// a group's in-partition values and 16-bit local columns (ecap entries each, filled
+// Shared memory of the register smoother: two mbarriers, x twice (each buffer holds
+// kXCopies copies of the group's x, xcopy_stride<T>() elements apart), then two staging
+// buffers for a group's in-partition values and 16-bit columns (ecap entries each, filled
 // as 16-byte rounded ranges).
 struct RegSmemLayout {
   size_t x0, x1, val0, col0, val1, col1, total;
@@ -349,9 +349,10 @@ __host__ __device__ constexpr size_t round16(size_t v) {
 template <class T>
 __host__ __device__ inline RegSmemLayout reg_smem_layout(int ecap) {
   RegSmemLayout L{};
+  constexpr size_t xbytes = (size_t)kXCopies * xcopy_stride<T>() * sizeof(T);
   L.x0 = 16;
-  L.x1 = L.x0 + (size_t)(kRegGroupRows + 1) * sizeof(T);
-  L.val0 = round16<T>(L.x1 + (size_t)(kRegGroupRows + 1) * sizeof(T));
+  L.x1 = L.x0 + xbytes;
+  L.val0 = round16<T>(L.x1 + xbytes);
   L.col0 = round16<T>(L.val0 + (size_t)ecap * sizeof(T));
   L.val1 = round16<T>(L.col0 + (size_t)ecap * 2);
   L.col1 = round16<T>(L.val1 + (size_t)ecap * sizeof(T));
@@ -360,31 +361,38 @@ __host__ __device__ inline RegSmemLayout reg_smem_layout(int ecap) {
 }
 
 // One thread (thread 0) starts the bulk copies of group g's values and columns into
-// staging buffer `buf`; completion is counted on bar[buf].
+// staging buffer `buf`; completion is counted on bar[buf].  The group's entries are one
+// contiguous range in the jagged-diagonal arrays (the reordering stays inside each
+// 32-row block).
 template <class T>
 __device__ __forceinline__ void stage_group(unsigned char* sm, const RegSmemLayout& Ls, uint64_t* bar, int buf,
                                             int g, const int32_t* __restrict__ grows,
-                                            const int32_t* __restrict__ irp, const uint16_t* __restrict__ c16,
-                                            const T* __restrict__ iv) {
+                                            const int32_t* __restrict__ irp, const uint16_t* __restrict__ jc,
+                                            const T* __restrict__ jv) {
   constexpr int VA = 16 / (int)sizeof(T);
   const int es = irp[grows[g]], ee = irp[grows[g + 1]];
   const int v0 = es & ~(VA - 1), c0 = es & ~7;
   const uint32_t vbytes = (uint32_t)((((ee + VA - 1) & ~(VA - 1)) - v0) * (int)sizeof(T));
   const uint32_t cbytes = (uint32_t)((((ee + 7) & ~7) - c0) * 2);
   mbar_arrive_expect_tx(bar + buf, vbytes + cbytes);
-  if (vbytes) bulk_copy_g2s(sm + (buf ? Ls.val1 : Ls.val0), iv + v0, vbytes, bar + buf);
-  if (cbytes) bulk_copy_g2s(sm + (buf ? Ls.col1 : Ls.col0), c16 + c0, cbytes, bar + buf);
+  if (vbytes) bulk_copy_g2s(sm + (buf ? Ls.val1 : Ls.val0), jv + v0, vbytes, bar + buf);
+  if (cbytes) bulk_copy_g2s(sm + (buf ? Ls.col1 : Ls.col0), jc + c0, cbytes, bar + buf);
 }
 
 // Register-resident smoother for groups of at most 512 rows whose in-partition rows
 // have at most K entries: one thread per row, persistent CTAs walking the groups.
 // A group's values and 16-bit local columns are contiguous in HBM; thread 0 moves the
 // NEXT group's ranges into the other staging buffer with bulk asynchronous copies
-// (TMA) while the CTA smooths the current one.  Each thread keeps its row's entries
-// (padded to K with zero values pointing at a zero slot of x) in registers across the
-// sweeps; x is double-buffered in shared memory (one barrier per sweep).  Row sums
-// are the one-lane case of the shared-memory smoother: fused multiply-adds in entry
-// order.  A copy that does not land within the wait limit sets *kerr and ends the CTA.
+// (TMA) while the CTA smooths the current one.  Lane p of the warp that owns a 32-row
+// block smooths the block's row at sorted position p (rows by decreasing length), and
+// the entries are stored diagonal by diagonal, so the lanes read their k-th entries
+// from consecutive shared-memory words.  Each thread keeps its row's entries in
+// registers across the sweeps; x is double-buffered in shared memory, kXCopies copies
+// per buffer, every entry's column pointing into the copy that setup chose to spread the
+// warp's gathers over the banks (one barrier per sweep).  Row sums are the one-lane case
+// of the shared-memory smoother: fused multiply-adds in entry order.  A copy that does
+// not land within `wait_limit` polls sets *kerr and ends the CTA after waiting (with the
+// full limit) for the copies it has in flight.
 // Level-0 fusions (each off when its pointer is null):
 // - pre relax, b64: the right-hand side is read in FP64 and rounded to T here (and
 //   stored to b_store for the post relax) instead of by a separate cast;
@@ -398,13 +406,13 @@ __device__ __forceinline__ void stage_group(unsigned char* sm, const RegSmemLayo
 template <class T, bool POST, int K>
 __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
     int ngroups, const int32_t* __restrict__ grows, const int32_t* __restrict__ irp,
-    const uint16_t* __restrict__ c16, const T* __restrict__ iv, const T* __restrict__ diag,
-    const T* __restrict__ dinv, const T* __restrict__ b, T w, int inner, const T* __restrict__ x_in,
-    T* __restrict__ x_out, T* __restrict__ r_out, int ecap, double* __restrict__ kerr,
+    const uint16_t* __restrict__ jc, const T* __restrict__ jv, const uint8_t* __restrict__ jrow,
+    const T* __restrict__ diag, const T* __restrict__ dinv, const T* __restrict__ b, T w, int inner,
+    const T* __restrict__ x_in, T* __restrict__ x_out, T* __restrict__ r_out, int ecap, double* __restrict__ kerr,
     const double* __restrict__ b64, T* __restrict__ b_store, const int32_t* __restrict__ orp,
     const int32_t* __restrict__ oci, const T* __restrict__ ov, double* __restrict__ z64,
     const double* __restrict__ dot_r, const double* __restrict__ dot_o, double* __restrict__ dot_part,
-    unsigned* dot_count, double* sc, int flexible) {
+    unsigned* dot_count, double* sc, int flexible, int wait_limit) {
   extern __shared__ __align__(128) unsigned char sm[];
   __shared__ double sh_dot[32];
   double dz1 = 0.0, dz2 = 0.0;
@@ -412,27 +420,27 @@ __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
   uint64_t* bar = reinterpret_cast<uint64_t*>(sm);
   T* const xa = reinterpret_cast<T*>(sm + Ls.x0);
   T* const xb = reinterpret_cast<T*>(sm + Ls.x1);
-  constexpr int kZero = kRegGroupRows;  // x slot that stays 0
+  constexpr int CS = xcopy_stride<T>();
   constexpr int VA = 16 / (int)sizeof(T);
-  const int t = threadIdx.x;
+  const int t = threadIdx.x, lane = t & 31;
   if (t == 0) {
     mbar_init(bar, 1);
     mbar_init(bar + 1, 1);
-    xa[kZero] = (T)0;
-    xb[kZero] = (T)0;
   }
   __syncthreads();
-  if (t == 0 && (int)blockIdx.x < ngroups) stage_group<T>(sm, Ls, bar, 0, blockIdx.x, grows, irp, c16, iv);
+  if (t == 0 && (int)blockIdx.x < ngroups) stage_group<T>(sm, Ls, bar, 0, blockIdx.x, grows, irp, jc, jv);
   int i = 0;
   for (int g = blockIdx.x; g < ngroups; g += gridDim.x, i++) {
     const int buf = i & 1;
     const uint32_t parity = (uint32_t)(i >> 1) & 1u;
     const int gn = g + gridDim.x;
     // buffer buf ^ 1 was last read before the barrier that ended the previous group
-    if (t == 0 && gn < ngroups) stage_group<T>(sm, Ls, bar, buf ^ 1, gn, grows, irp, c16, iv);
+    if (t == 0 && gn < ngroups) stage_group<T>(sm, Ls, bar, buf ^ 1, gn, grows, irp, jc, jv);
     const int rs = grows[g], re = grows[g + 1];
-    const bool live = t < re - rs;
-    const int row = rs + t;
+    const int wb = rs + (t & ~31);  // first row of this warp's 32-row block
+    const bool live = rs + t < re;
+    const int row = live ? wb + jrow[rs + t] : rs;
+    const int loc = row - rs;
     int e0 = 0, len = 0;
     T d = (T)1, di = (T)1, bb = (T)0, x = (T)0;
     double dr = 0.0, dor = 0.0;  // the dot operands, loaded now so the sweeps hide their latency
@@ -458,20 +466,29 @@ __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
         }
         x = (w * bb) * di;
       }
-      xa[t] = x;
+#pragma unroll
+      for (int c = 0; c < kXCopies; c++) xa[loc + c * CS] = x;
     }
-    const bool ok = mbar_wait_bounded(bar + buf, parity);
+    const int kmax = __shfl_sync(0xffffffffu, len, 0);  // lane 0 holds the block's longest row
+    const bool ok = mbar_wait_bounded(bar + buf, parity, wait_limit);
     T val[K];
-    uint32_t off[K];
+    uint32_t offp[K / 2];  // two 16-bit columns per register
     {
       const int es = irp[rs];
-      const T* sval = reinterpret_cast<const T*>(sm + (buf ? Ls.val1 : Ls.val0)) + (e0 - (es & ~(VA - 1)));
-      const uint16_t* scol = reinterpret_cast<const uint16_t*>(sm + (buf ? Ls.col1 : Ls.col0)) + (e0 - (es & ~7));
+      // the block's entries start where its first row's do (the reordering stays in the block)
+      const int eb = live ? irp[wb] : 0;
+      const T* sval = reinterpret_cast<const T*>(sm + (buf ? Ls.val1 : Ls.val0)) + (eb - (es & ~(VA - 1)));
+      const uint16_t* scol = reinterpret_cast<const uint16_t*>(sm + (buf ? Ls.col1 : Ls.col0)) + (eb - (es & ~7));
+      int dk = lane;  // this lane's position on diagonal k
 #pragma unroll
       for (int k = 0; k < K; k++) {
+        const unsigned m = __ballot_sync(0xffffffffu, k < len);
         const bool a = ok && k < len;
-        val[k] = a ? sval[k] : (T)0;
-        off[k] = a ? (uint32_t)scol[k] : (uint32_t)kZero;
+        val[k] = a ? sval[dk] : (T)0;
+        const uint32_t o = a ? (uint32_t)scol[dk] : 0u;
+        if (k & 1) offp[k >> 1] |= o << 16;
+        else offp[k >> 1] = o;
+        dk += __popc(m);
       }
     }
     if (__syncthreads_or(!ok)) {
@@ -483,13 +500,18 @@ __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
       }
       return;
     }
+    auto rowsum = [&](const T* src) {
+      T sax = 0;
+#pragma unroll
+      for (int k = 0; k < K; k++)
+        if (k < kmax && k < len) sax = fma(val[k], src[(offp[k >> 1] >> ((k & 1) * 16)) & 0xffffu], sax);
+      return sax;
+    };
     auto sweep = [&](const T* src, T* dst) {
       if (live) {
-        T sax = 0;
+        x = relax(x, bb, rowsum(src), d, di, w);
 #pragma unroll
-        for (int k = 0; k < K; k++) sax = fma(val[k], src[off[k]], sax);
-        x = relax(x, bb, sax, d, di, w);
-        dst[t] = x;
+        for (int c = 0; c < kXCopies; c++) dst[loc + c * CS] = x;
       }
       __syncthreads();
     };
@@ -515,10 +537,7 @@ __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
         x_out[row] = x;
       }
       if (!POST) {
-        T sax = 0;
-#pragma unroll
-        for (int k = 0; k < K; k++) sax = fma(val[k], last[off[k]], sax);
-        T u = bb - sax;
+        T u = bb - rowsum(last);
         r_out[row] = u - d * x;
       }
     }
@@ -1172,11 +1191,11 @@ void smooth_sweeps(Ctx& c, Level<T>& L, bool post, const T* b, const T* xin, T* 
     auto k = post ? smooth_reg_kernel<T, true, kRegRow> : smooth_reg_kernel<T, false, kRegRow>;
     if (L.smooth_smem > 48 * 1024)
       ensure_smem(k, L.smooth_smem);
-    FG_LAUNCH(k, L.smooth_grid, L.smooth_threads, L.smooth_smem, s, L.ngroups, L.grows.p, L.Ain.rp.p, L.ci16.p,
-              L.Ain.v.p, L.diag.p, L.dinv.p, b, w, inner, xin, xout, rout, L.max_group_ents + 16,
+    FG_LAUNCH(k, L.smooth_grid, L.smooth_threads, L.smooth_smem, s, L.ngroups, L.grows.p, L.Ain.rp.p, L.jc16.p,
+              L.jv.p, L.jrow.p, L.diag.p, L.dinv.p, b, w, inner, xin, xout, rout, L.max_group_ents + 16,
               c.red.p + 2 * kRedBlocks + S_KERR, f.b64, f.b_store, f.aout ? L.Aout.rp.p : nullptr,
               f.aout ? L.Aout.ci.p : nullptr, f.aout ? L.Aout.v.p : nullptr, f.z64, f.dot_r, f.dot_o, f.dot_part,
-              c.rcount.p + 3, c.red.p + 2 * kRedBlocks, f.dot_o ? 1 : 0);
+              c.rcount.p + 3, c.red.p + 2 * kRedBlocks, f.dot_o ? 1 : 0, c.copy_wait_limit);
     return;
   }
   if (L.smooth_k > 0) {
@@ -1724,27 +1743,59 @@ void profile_level0(Ctx& c, Hierarchy<T>& H, int which, int reps, double* ms, do
   FG_LAUNCH(fill_value_kernel<T>, grid_for(n, 256), 256, 0, s, (int64_t)n, L.x.p, (T)0.5);
   FG_LAUNCH(fill_value_kernel<T>, grid_for(n, 256), 256, 0, s, (int64_t)n, L.r.p, (T)0.25);
   FG_LAUNCH(fill_value_kernel<T>, grid_for(L.nagg, 256), 256, 0, s, (int64_t)L.nagg, L.t.p, (T)0.125);
+  if (which == 5) {
+    ensure_work(c, c.A.n);
+    FG_LAUNCH(fill_value_kernel<double>, grid_for(n, 256), 256, 0, s, (int64_t)n, c.vr.p, 0.5);
+    FG_LAUNCH(fill_value_kernel<double>, grid_for(n, 256), 256, 0, s, (int64_t)n, c.vrold.p, 0.25);
+  }
   auto run = [&]() {
     switch (which) {
       case 1: smooth<T>(c, L, false, L.b.p, nullptr, L.x.p, L.r.p); break;
       case 2: smooth_sweeps<T>(c, L, true, L.bp.p, L.x.p, L.xo.p, nullptr); break;
       case 3: spmv_lanes(L.R, L.r.p, L.t.p, 0, s); break;
+      case 5: {
+        // the last post relax of a PCG iteration's V-cycle: b - A_out x, the sweeps, z
+        // widened to FP64 and the z.r / z.r_old partials with beta from the last CTA
+        Ctx::ZDot zd;
+        zd.r = c.vr.p;
+        zd.rold = c.vrold.p;
+        zd.part = c.red.p;
+        c.zdot = &zd;
+        try {
+          smooth<T>(c, L, true, L.b.p, L.x.p, L.xo.p, nullptr, nullptr, nullptr, c.vz.p);
+        } catch (...) {
+          c.zdot = nullptr;
+          throw;
+        }
+        c.zdot = nullptr;
+        if (!zd.done)
+          FG_LAUNCH(dot_beta_kernel, kRedBlocks, kRedThreads, 0, s, n, c.vz.p, c.vr.p, c.vrold.p, c.red.p,
+                    c.red.p + kRedBlocks, c.red.p + 2 * kRedBlocks, 1, c.rcount.p);
+        break;
+      }
       default: spmv_lanes(L.P, L.t.p, L.xo.p, 1, s); break;
     }
   };
   if (which == 2)  // the post relax's right-hand side, computed once outside the timing
     aout_rhs<T>(s, L, L.b.p, L.x.p, L.bp.p);
-  // in-partition entries: value + 16-bit column on the register path, + 32-bit column otherwise
-  const double ein = smoother_in_registers(L.max_in_row, L.max_part_rows) ? ts + 2 : ts + 4;
+  // in-partition entries: value + 16-bit column on the register path (plus one byte per
+  // row for its place in its block), value + 32-bit column otherwise
+  const bool reg = smoother_in_registers(L.max_in_row, L.max_part_rows);
+  const double ein = reg ? ts + 2 : ts + 4;
+  const double rowb = reg ? 1.0 * n : 0.0;
   switch (which) {
     case 1:  // entries, row offsets, b, diag, 1/diag in; x, r out
-      *bytes = L.Ain.nnz * ein + 4.0 * (n + 1) + 3 * ts * n + 2 * ts * n;
+      *bytes = L.Ain.nnz * ein + 4.0 * (n + 1) + 3 * ts * n + 2 * ts * n + rowb;
       break;
     case 2:  // entries, row offsets, b', diag, 1/diag, x in; x out
-      *bytes = L.Ain.nnz * ein + 4.0 * (n + 1) + 4 * ts * n + ts * n;
+      *bytes = L.Ain.nnz * ein + 4.0 * (n + 1) + 4 * ts * n + ts * n + rowb;
       break;
     case 3:
       *bytes = L.R.nnz * (ts + 4) + 4.0 * (L.nagg + 1) + ts * n + ts * L.nagg;
+      break;
+    case 5:  // as case 2 plus A_out (entries, row offsets) for b - A_out x, z out in FP64, r and r_old in
+      *bytes = L.Ain.nnz * ein + 4.0 * (n + 1) + 4 * ts * n + L.Aout.nnz * (ts + 4) + 4.0 * (n + 1) + 8.0 * n +
+               16.0 * n + rowb;
       break;
     default:
       *bytes = L.P.nnz * (ts + 4) + 4.0 * (n + 1) + ts * L.nagg + 2 * ts * n;
@@ -1771,10 +1822,16 @@ void profile_level0(Ctx& c, Hierarchy<T>& H, int which, int reps, double* ms, do
 // Times one hot kernel with CUDA events on the handle's stream (after 3 untimed
 // launches) and reports its algorithmic bytes: 0 = the outer PCG's FP64 SpMV
 // (CSR, fused dot), 1 = level-0 pre-smoother, 2 = level-0 post-smoother relax,
-// 3 = level-0 restriction R r, 4 = level-0 prolongation x += P xc.
+// 3 = level-0 restriction R r, 4 = level-0 prolongation x += P xc, 5 = the level-0
+// post-smoother as a PCG iteration runs it (fused), 6 / 7 = the assembly's element and
+// row-gather kernels.
 void profile_kernel(Ctx& c, int which, int reps, double* ms, double* bytes) {
+  FG_REQUIRE(reps > 0 && which >= 0 && which <= 7, FEMGPU_ERR_INVALID, "bad kernel selector");
+  if (which == 6 || which == 7) {
+    profile_assembly(c, which, reps, ms, bytes);
+    return;
+  }
   FG_REQUIRE(c.has_hierarchy, FEMGPU_ERR_NOT_READY, "call femgpu_setup first");
-  FG_REQUIRE(reps > 0 && which >= 0 && which <= 4, FEMGPU_ERR_INVALID, "bad kernel selector");
   cudaStream_t s = c.stream;
   if (which == 0) {
     const int n = c.A.n;

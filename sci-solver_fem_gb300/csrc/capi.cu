@@ -438,12 +438,25 @@ femgpu_status femgpu_solve_multi_device(femgpu_handle h, int nrhs, const double*
     FG_CUDA(cudaEventRecord(e0, h->stream));
     int iters = 0;
     double worst = 0.0;
-    for (int j = 0; j < nrhs; j++) {
-      // one hierarchy, one captured PCG loop, one column at a time
-      SolveResult r = amg_solve_device(*h, d_B + j * ldb, d_X + j * ldx);
-      iters += r.iterations;
-      worst = std::max(worst, r.relres);
-      if (r.status != FEMGPU_OK && result == FEMGPU_OK) result = r.status;
+    if (h->cfg.solverType == 1) {
+      // PCG: the columns eight at a time, each block in lockstep with SpMM kernels
+      std::vector<int> it(nrhs);
+      std::vector<double> rr(nrhs);
+      std::vector<femgpu_status> stc(nrhs, FEMGPU_OK);
+      block_solve_device(*h, nrhs, d_B, ldb, d_X, ldx, it.data(), rr.data(), stc.data());
+      for (int j = 0; j < nrhs; j++) {
+        iters += it[j];
+        worst = std::max(worst, rr[j]);
+        if (stc[j] != FEMGPU_OK && result == FEMGPU_OK) result = stc[j];
+      }
+    } else {
+      for (int j = 0; j < nrhs; j++) {
+        // one V-cycle per column (AMG_SOLVER)
+        SolveResult r = amg_solve_device(*h, d_B + j * ldb, d_X + j * ldx);
+        iters += r.iterations;
+        worst = std::max(worst, r.relres);
+        if (r.status != FEMGPU_OK && result == FEMGPU_OK) result = r.status;
+      }
     }
     FG_CUDA(cudaEventRecord(e1, h->stream));
     FG_CUDA(cudaEventSynchronize(e1));
@@ -640,6 +653,13 @@ femgpu_status femgpu_vcycle(femgpu_handle h, const double* r, double* z) {
 femgpu_status femgpu_profile_kernel(femgpu_handle h, int which, int reps, double* avg_ms, double* bytes) {
   if (!h || !avg_ms || !bytes) return FEMGPU_ERR_INVALID;
   return guard(h, [&] { profile_kernel(*h, which, reps, avg_ms, bytes); });
+}
+
+femgpu_status femgpu_test_copy_wait_limit(femgpu_handle h, int polls) {
+  if (!h) return FEMGPU_ERR_INVALID;
+  h->copy_wait_limit = polls < 0 ? kMbarWaitLimit : polls;
+  h->hier_gen++;  // the captured PCG loop holds the old limit: capture it again
+  return FEMGPU_OK;
 }
 
 femgpu_status femgpu_kernel_launches(femgpu_handle h, int64_t* count) {

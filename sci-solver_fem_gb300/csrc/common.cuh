@@ -242,10 +242,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return done != 0;
 }
 
-// Waits for the barrier phase with an iteration limit; false when it ran out.
+// Waits for the barrier phase with an iteration limit; false when it ran out (a limit
+// of 0 gives up without polling).
 constexpr int kMbarWaitLimit = 1 << 22;
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-  for (int i = 0; i < kMbarWaitLimit; i++)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int limit = kMbarWaitLimit) {
+  for (int i = 0; i < limit; i++)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }

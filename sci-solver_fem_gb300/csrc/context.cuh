@@ -56,9 +56,18 @@ struct Level {
   // smoother work groups: consecutive partitions packed per CTA (row offsets)
   DBuf<int32_t> grows;
   int ngroups = 0, max_group_rows = 0, max_group_ents = 0;
-  // register smoother: in-partition columns relative to their group's first row
-  // (16 bit), padded by 16 entries like Ain.v so 16-byte rounded copies stay inside
-  DBuf<uint16_t> ci16;
+  // register smoother: the in-partition entries of every 32-row block of a group in
+  // jagged-diagonal order (the block's rows sorted by decreasing length, stable; entry k
+  // of the row at sorted position p sits at (block's first entry) + (entries of the
+  // block's diagonals 0..k-1) + p), so lane p of a warp reads its entries from consecutive
+  // addresses.  jv: values; jc16: the column relative to the group's first row plus
+  // c * xcopy_stride<T>() for the copy of x the entry reads (chosen at setup to spread a
+  // warp's gathers over the shared-memory banks); jrow: per slot of a block, the sorted
+  // row's offset in the block.  jv and jc16 carry 16 entries of slack like Ain.v, so
+  // 16-byte rounded bulk copies stay inside.
+  DBuf<T> jv;
+  DBuf<uint16_t> jc16;
+  DBuf<uint8_t> jrow;
   // shared-memory smoother plan: lanes per row, CTAs per cluster (one cluster per
   // group), rows and entries of the largest CTA row slice, launch shape
   int smooth_lanes = 1, cluster = 1, slice_rows = 0, slice_ents = 0, smooth_threads = 0, smooth_grid = 0;
@@ -75,6 +84,14 @@ struct Level {
 // partitions of at most 512 rows (one thread per row).
 constexpr int kRegRow = 16;
 constexpr int kRegGroupRows = 512;
+// The register smoother keeps kXCopies copies of the group's x in shared memory,
+// xcopy_stride<T>() elements apart: a stride 32 bytes past a multiple of 128 bytes, so
+// copy c of an element sits 8c banks further on.  Slot kRegGroupRows of copy 0 is spare.
+constexpr int kXCopies = 4;
+template <class T>
+__host__ __device__ constexpr int xcopy_stride() {
+  return sizeof(T) == 4 ? 520 : 516;
+}
 inline bool smoother_in_registers(int max_in_row, int max_part_rows) {
   return max_in_row <= kRegRow && max_part_rows <= kRegGroupRows;
 }
@@ -103,6 +120,11 @@ struct Hierarchy : HierarchyBase {
   std::vector<std::unique_ptr<Level<T>>> L;
 };
 
+// Work state of the multi-right-hand-side solve (block_solve.cu), kept per handle.
+struct BlockStateBase {
+  virtual ~BlockStateBase() {}
+};
+
 struct Ctx {
   femgpu_config cfg{};
   int device = 0;
@@ -115,6 +137,7 @@ struct Ctx {
   Mesh mesh;
   bool has_mesh = false;
   DBuf<double> coef;             // per-element coefficients of the last femgpu_assemble (empty: labels / 1)
+  double lambda_mass = 0.0;      // mass weight of the last femgpu_assemble
   DBuf<uint8_t> dmask;           // Dirichlet mask of the last femgpu_set_dirichlet (empty: none)
   bool assembled_from_mesh = false;
   DCsr<double> A;                // level-0 operator, original numbering, FP64
@@ -154,6 +177,14 @@ struct Ctx {
     bool done = false;
   };
   ZDot* zdot = nullptr;
+  // polls of the register smoother's wait for its staged entries before it gives up
+  // (femgpu_test_copy_wait_limit lowers it to exercise the error path)
+  int copy_wait_limit = kMbarWaitLimit;
+  // block vectors and scalars of the multi-right-hand-side solve, rebuilt with the hierarchy
+  std::unique_ptr<BlockStateBase> block;
+  // device address of the no-alloc load vector's built-in scratch region, looked up by
+  // the first such call on this handle (a handle lives in one device context)
+  double* noalloc_scratch = nullptr;
   // stage timing of a V-cycle run outside capture (FEMGPU_PROFILE set): named events
   std::vector<std::pair<std::string, cudaEvent_t>>* stage_marks = nullptr;
 
@@ -174,6 +205,11 @@ void apply_dirichlet(Ctx& c, const uint8_t* mask_host);
 void zero_dirichlet_rows(Ctx& c, const double* d_in, double* d_out);
 // dL/dtheta_e = -c_e lambda_e^T K_e u_e for theta_e = log c_e (per element, device arrays).
 void element_log_coef_gradient(Ctx& c, const double* d_lam, const double* d_u, double* d_grad);
+// Times the assembly's element kernel (which = 6) or row-gather kernel (which = 7) with
+// CUDA events on c.stream for the current mesh and coefficients, writing into scratch
+// buffers (the operator is left as it is); reports the average time and the algorithmic
+// bytes per launch.
+void profile_assembly(Ctx& c, int which, int reps, double* ms, double* bytes);
 
 // amg_setup.cu
 void amg_setup(Ctx& c);
@@ -196,5 +232,11 @@ void plan_smoother(Ctx& c, Level<T>& L);
 void amg_vcycle_device(Ctx& c, const double* d_r, double* d_z);
 void spmv_original(Ctx& c, const double* d_x, double* d_y);
 void profile_kernel(Ctx& c, int which, int reps, double* ms, double* bytes);
+
+// block_solve.cu: nrhs right-hand sides (column j at d_B + j * ldb, initial guesses and
+// solutions at d_X + j * ldx), eight at a time in lockstep PCGs whose operator and V-cycle
+// applications are block (SpMM) kernels; per column: iterations, relative residual, status.
+void block_solve_device(Ctx& c, int nrhs, const double* d_B, int64_t ldb, double* d_X, int64_t ldx, int* iters,
+                        double* relres, femgpu_status* status);
 
 }  // namespace femgpu

@@ -10,7 +10,9 @@
 // into a per-element table; one thread per row then gathers its entries from the
 // incident elements in element order.  No floating-point atomics: the sum at
 // every slot is taken in element order, so results are bitwise reproducible and
-// equal to a sequential element loop.
+// equal to a sequential element loop.  Tetrahedra use a fused multiply-add gradient
+// formulation (tet_gradients), within a few units in the last place of the reference's
+// cofactor inverse; triangles follow the reference's arithmetic.
 #include "context.cuh"
 #include "quadrature.h"
 
@@ -26,40 +28,6 @@ __device__ __forceinline__ int upper_index(int a, int b, int k) {
   int i = a < b ? a : b, j = a < b ? b : a;
   return i * k - (i * (i - 1)) / 2 + (j - i);
 }
-
-// 4x4 cofactor expansion terms (row*4 + col of the matrix [x y z 1] per vertex),
-// evaluated in the order of perform_element_loop_3D.cuh:546-567 so that the FP64
-// inverse is bit-identical to the reference's.
-#define TE(r, c) (((r) - 1) * 4 + ((c) - 1))
-__constant__ unsigned char c_cof[16][6][3] = {
-  {{TE(2,2),TE(3,3),TE(4,4)},{TE(2,3),TE(3,4),TE(4,2)},{TE(2,4),TE(3,2),TE(4,3)},{TE(2,2),TE(3,4),TE(4,3)},{TE(2,3),TE(3,2),TE(4,4)},{TE(2,4),TE(3,3),TE(4,2)}},
-  {{TE(1,2),TE(3,4),TE(4,3)},{TE(1,3),TE(3,2),TE(4,4)},{TE(1,4),TE(3,3),TE(4,2)},{TE(1,2),TE(3,3),TE(4,4)},{TE(1,3),TE(3,4),TE(4,2)},{TE(1,4),TE(3,2),TE(4,3)}},
-  {{TE(1,2),TE(2,3),TE(4,4)},{TE(1,3),TE(2,4),TE(4,2)},{TE(1,4),TE(2,2),TE(4,3)},{TE(1,2),TE(2,4),TE(4,3)},{TE(1,3),TE(2,2),TE(4,4)},{TE(1,4),TE(2,3),TE(4,2)}},
-  {{TE(1,2),TE(2,4),TE(3,3)},{TE(1,3),TE(2,2),TE(3,4)},{TE(1,4),TE(2,3),TE(3,2)},{TE(1,2),TE(2,3),TE(3,4)},{TE(1,3),TE(2,4),TE(3,2)},{TE(1,4),TE(2,2),TE(3,3)}},
-  {{TE(2,1),TE(3,4),TE(4,3)},{TE(2,3),TE(3,1),TE(4,4)},{TE(2,4),TE(3,3),TE(4,1)},{TE(2,1),TE(3,3),TE(4,4)},{TE(2,3),TE(3,4),TE(4,1)},{TE(2,4),TE(3,1),TE(4,3)}},
-  {{TE(1,1),TE(3,3),TE(4,4)},{TE(1,3),TE(3,4),TE(4,1)},{TE(1,4),TE(3,1),TE(4,3)},{TE(1,1),TE(3,4),TE(4,3)},{TE(1,3),TE(3,1),TE(4,4)},{TE(1,4),TE(3,3),TE(4,1)}},
-  {{TE(1,1),TE(2,4),TE(4,3)},{TE(1,3),TE(2,1),TE(4,4)},{TE(1,4),TE(2,3),TE(4,1)},{TE(1,1),TE(2,3),TE(4,4)},{TE(1,3),TE(2,4),TE(4,1)},{TE(1,4),TE(2,1),TE(4,3)}},
-  {{TE(1,1),TE(2,3),TE(3,4)},{TE(1,3),TE(2,4),TE(3,1)},{TE(1,4),TE(2,1),TE(3,3)},{TE(1,1),TE(2,4),TE(3,3)},{TE(1,3),TE(2,1),TE(3,4)},{TE(1,4),TE(2,3),TE(3,1)}},
-  {{TE(2,1),TE(3,2),TE(4,4)},{TE(2,2),TE(3,4),TE(4,1)},{TE(2,4),TE(3,1),TE(4,2)},{TE(2,1),TE(3,4),TE(4,2)},{TE(2,2),TE(3,1),TE(4,4)},{TE(2,4),TE(3,2),TE(4,1)}},
-  {{TE(1,1),TE(3,4),TE(4,2)},{TE(1,2),TE(3,1),TE(4,4)},{TE(1,4),TE(3,2),TE(4,1)},{TE(1,1),TE(3,2),TE(4,4)},{TE(1,2),TE(3,4),TE(4,1)},{TE(1,4),TE(3,1),TE(4,2)}},
-  {{TE(1,1),TE(2,2),TE(4,4)},{TE(1,2),TE(2,4),TE(4,1)},{TE(1,4),TE(2,1),TE(4,2)},{TE(1,1),TE(2,4),TE(4,2)},{TE(1,2),TE(2,1),TE(4,4)},{TE(1,4),TE(2,2),TE(4,1)}},
-  {{TE(1,1),TE(2,4),TE(3,2)},{TE(1,2),TE(2,1),TE(3,4)},{TE(1,4),TE(2,2),TE(3,1)},{TE(1,1),TE(2,2),TE(3,4)},{TE(1,2),TE(2,4),TE(3,1)},{TE(1,4),TE(2,1),TE(3,2)}},
-  {{TE(2,1),TE(3,3),TE(4,2)},{TE(2,2),TE(3,1),TE(4,3)},{TE(2,3),TE(3,2),TE(4,1)},{TE(2,1),TE(3,2),TE(4,3)},{TE(2,2),TE(3,3),TE(4,1)},{TE(2,3),TE(3,1),TE(4,2)}},
-  {{TE(1,1),TE(3,2),TE(4,3)},{TE(1,2),TE(3,3),TE(4,1)},{TE(1,3),TE(3,1),TE(4,2)},{TE(1,1),TE(3,3),TE(4,2)},{TE(1,2),TE(3,1),TE(4,3)},{TE(1,3),TE(3,2),TE(4,1)}},
-  {{TE(1,1),TE(2,3),TE(4,2)},{TE(1,2),TE(2,1),TE(4,3)},{TE(1,3),TE(2,2),TE(4,1)},{TE(1,1),TE(2,2),TE(4,3)},{TE(1,2),TE(2,3),TE(4,1)},{TE(1,3),TE(2,1),TE(4,2)}},
-  {{TE(1,1),TE(2,2),TE(3,3)},{TE(1,2),TE(2,3),TE(3,1)},{TE(1,3),TE(2,1),TE(3,2)},{TE(1,1),TE(2,3),TE(3,2)},{TE(1,2),TE(2,1),TE(3,3)},{TE(1,3),TE(2,2),TE(3,1)}},
-};
-__constant__ unsigned char c_det[24][4] = {
-  {TE(1,1),TE(2,2),TE(3,3),TE(4,4)},{TE(1,1),TE(2,3),TE(3,4),TE(4,2)},{TE(1,1),TE(2,4),TE(3,2),TE(4,3)},
-  {TE(1,2),TE(2,1),TE(3,4),TE(4,3)},{TE(1,2),TE(2,3),TE(3,1),TE(4,4)},{TE(1,2),TE(2,4),TE(3,3),TE(4,1)},
-  {TE(1,3),TE(2,1),TE(3,2),TE(4,4)},{TE(1,3),TE(2,2),TE(3,4),TE(4,1)},{TE(1,3),TE(2,4),TE(3,1),TE(4,2)},
-  {TE(1,4),TE(2,1),TE(3,3),TE(4,2)},{TE(1,4),TE(2,2),TE(3,1),TE(4,3)},{TE(1,4),TE(2,3),TE(3,2),TE(4,1)},
-  {TE(1,1),TE(2,2),TE(3,4),TE(4,3)},{TE(1,1),TE(2,3),TE(3,2),TE(4,4)},{TE(1,1),TE(2,4),TE(3,3),TE(4,2)},
-  {TE(1,2),TE(2,1),TE(3,3),TE(4,4)},{TE(1,2),TE(2,3),TE(3,4),TE(4,1)},{TE(1,2),TE(2,4),TE(3,1),TE(4,3)},
-  {TE(1,3),TE(2,1),TE(3,4),TE(4,2)},{TE(1,3),TE(2,2),TE(3,1),TE(4,4)},{TE(1,3),TE(2,4),TE(3,2),TE(4,1)},
-  {TE(1,4),TE(2,1),TE(3,2),TE(4,3)},{TE(1,4),TE(2,2),TE(3,3),TE(4,1)},{TE(1,4),TE(2,3),TE(3,1),TE(4,2)},
-};
-#undef TE
 
 __device__ __forceinline__ double label_coef(int label) {
   // co of element_loop_3d_kernel (perform_element_loop_3D.cuh:585-612)
@@ -125,74 +93,68 @@ __global__ void graph_from_pattern_kernel(const int32_t* rowptr, const int32_t* 
 }
 
 // ---- assembly --------------------------------------------------------------------
-// Vertex coordinates, volume and P1 basis gradients g[a] of tetrahedron e (the
-// cofactor inverse of perform_element_loop_3D.cuh:525-583, terms in its order).
-__device__ __forceinline__ void tet_basis(const double* __restrict__ xyz, const int32_t* __restrict__ conn,
-                                          int64_t e, double x[4], double y[4], double z[4], double& vol,
-                                          double g[4][3]) {
-  int id[4];
+// P1 basis gradients of tetrahedron e from its edge vectors (a fused multiply-add
+// formulation; the CPU oracle evaluates the same operations in the same order):
+// with a = p1 - p0, b = p2 - p0, c = p3 - p0 and det = a . (b x c),
+// grad l1 = (b x c) / det, grad l2 = (c x a) / det, grad l3 = (a x b) / det,
+// grad l0 = -((grad l1 + grad l2) + grad l3); the volume is |det| / 6.  About a quarter of
+// the floating-point work of the 4x4 cofactor inverse (perform_element_loop_3D.cuh:
+// 525-583), which it matches to a few units in the last place.
+__device__ __forceinline__ void cross_fma(const double u[3], const double v[3], double w[3]) {
+  w[0] = fma(u[1], v[2], -(u[2] * v[1]));
+  w[1] = fma(u[2], v[0], -(u[0] * v[2]));
+  w[2] = fma(u[0], v[1], -(u[1] * v[0]));
+}
+
+__device__ __forceinline__ void tet_gradients(const double* __restrict__ xyz, const int32_t* __restrict__ conn,
+                                              int64_t e, double& det, double g[4][3]) {
+  double p[4][3];
 #pragma unroll
-  for (int a = 0; a < 4; a++) {
-    id[a] = conn[e * 4 + a];
-    x[a] = xyz[(int64_t)id[a] * 3];
-    y[a] = xyz[(int64_t)id[a] * 3 + 1];
-    z[a] = xyz[(int64_t)id[a] * 3 + 2];
+  for (int q = 0; q < 4; q++) {
+    const int64_t v = conn[e * 4 + q];
+#pragma unroll
+    for (int d = 0; d < 3; d++) p[q][d] = xyz[v * 3 + d];
   }
-  double a1 = x[1] - x[3], a2 = y[1] - y[3], a3 = z[1] - z[3];
-  double b1 = x[2] - x[3], b2 = y[2] - y[3], b3 = z[2] - z[3];
-  double c1 = x[0] - x[3], c2 = y[0] - y[3], c3 = z[0] - z[3];
-  vol = fabs(c1 * (a2 * b3 - a3 * b2) + c2 * (a3 * b1 - a1 * b3) + c3 * (a1 * b2 - a2 * b1)) / 6.0;
-  double m[16];
+  double a[3], b[3], c[3], bc[3], ca[3], ab[3];
 #pragma unroll
-  for (int r = 0; r < 4; r++) {
-    m[r * 4 + 0] = x[r];
-    m[r * 4 + 1] = y[r];
-    m[r * 4 + 2] = z[r];
-    m[r * 4 + 3] = 1.0;
+  for (int d = 0; d < 3; d++) {
+    a[d] = p[1][d] - p[0][d];
+    b[d] = p[2][d] - p[0][d];
+    c[d] = p[3][d] - p[0][d];
   }
-  double det = m[c_det[0][0]] * m[c_det[0][1]] * m[c_det[0][2]] * m[c_det[0][3]];
+  cross_fma(b, c, bc);
+  cross_fma(c, a, ca);
+  cross_fma(a, b, ab);
+  det = fma(a[0], bc[0], fma(a[1], bc[1], a[2] * bc[2]));
+  const double inv = 1.0 / det;
 #pragma unroll
-  for (int t = 1; t < 24; t++) {
-    double p = m[c_det[t][0]] * m[c_det[t][1]] * m[c_det[t][2]] * m[c_det[t][3]];
-    det = t < 12 ? det + p : det - p;
-  }
-#pragma unroll
-  for (int kk = 0; kk < 4; kk++) {
-#pragma unroll
-    for (int mm = 0; mm < 3; mm++) {
-      const unsigned char(*T)[3] = c_cof[mm * 4 + kk];
-      double s = m[T[0][0]] * m[T[0][1]] * m[T[0][2]];
-      s = s + m[T[1][0]] * m[T[1][1]] * m[T[1][2]];
-      s = s + m[T[2][0]] * m[T[2][1]] * m[T[2][2]];
-      s = s - m[T[3][0]] * m[T[3][1]] * m[T[3][2]];
-      s = s - m[T[4][0]] * m[T[4][1]] * m[T[4][2]];
-      s = s - m[T[5][0]] * m[T[5][1]] * m[T[5][2]];
-      g[kk][mm] = s / det;
-    }
+  for (int d = 0; d < 3; d++) {
+    g[1][d] = bc[d] * inv;
+    g[2][d] = ca[d] * inv;
+    g[3][d] = ab[d] * inv;
+    g[0][d] = -((g[1][d] + g[2][d]) + g[3][d]);
   }
 }
 
+// Element matrices of P1 tetrahedra: the 10 upper-triangle entries of co K_e + lambda M_e
+// (perform_element_loop_3D.cuh:28-116,480-627): K_ab = vol grad l_a . grad l_b, the mass
+// from the reference-element integrand table times |det| / 8.
 __global__ void element3d_kernel(const double* __restrict__ xyz, const int32_t* __restrict__ conn,
                                  const int32_t* __restrict__ labels, const double* __restrict__ coef, int64_t ne,
                                  double lambda, double* __restrict__ ev) {
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
-    double x[4], y[4], z[4], vol, g[4][3];
-    tet_basis(xyz, conn, e, x, y, z, vol, g);
-    const double X1 = x[0], Y1 = y[0], Z1 = z[0], X2 = x[1], Y2 = y[1], Z2 = z[1];
-    const double X3 = x[2], Y3 = y[2], Z3 = z[2], X4 = x[3], Y4 = y[3], Z4 = z[3];
-    double mdet = 0.125 * ((-X1 + X2) * (-Y1 + Y3) * (-Z1 + Z4) + (-Y1 + Y2) * (-Z1 + Z3) * (-X1 + X4) +
-                           (-Z1 + Z2) * (-X1 + X3) * (-Y1 + Y4) - (-X1 + X2) * (-Z1 + Z3) * (-Y1 + Y4) -
-                           (-Z1 + Z2) * (-Y1 + Y3) * (-X1 + X4) - (-Y1 + Y2) * (-X1 + X3) * (-Z1 + Z4));
-    double jac = fabs(mdet);
-    double co = coef ? coef[e] : (labels ? label_coef(labels[e]) : 1.0);
+    double det, g[4][3];
+    tet_gradients(xyz, conn, e, det, g);
+    const double co = coef ? coef[e] : (labels ? label_coef(labels[e]) : 1.0);
+    const double wk = (fabs(det) / 6.0) * co;
+    const double jac = fabs(det) * 0.125;
     int c = 0;
 #pragma unroll
     for (int kk = 0; kk < 4; kk++) {
 #pragma unroll
       for (int q = kk; q < 4; q++) {
-        double st = (g[kk][0] * g[q][0] + g[kk][1] * g[q][1] + g[kk][2] * g[q][2]) * vol * co;
-        double ms = c_tet_mass[c] * jac;
-        ev[(int64_t)c * ne + e] = st + lambda * ms;  // SoA: entry-major for coalesced stores
+        const double st = fma(g[kk][0], g[q][0], fma(g[kk][1], g[q][1], g[kk][2] * g[q][2])) * wk;
+        ev[(int64_t)c * ne + e] = fma(lambda, c_tet_mass[c] * jac, st);  // SoA: entry-major stores
         c++;
       }
     }
@@ -332,8 +294,9 @@ __global__ void grad3d_kernel(const double* __restrict__ xyz, const int32_t* __r
                               const double* __restrict__ lam, const double* __restrict__ u,
                               double* __restrict__ grad) {
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
-    double x[4], y[4], z[4], vol, g[4][3];
-    tet_basis(xyz, conn, e, x, y, z, vol, g);
+    double det, g[4][3];
+    tet_gradients(xyz, conn, e, det, g);
+    const double vol = fabs(det) / 6.0;
     double gl[3] = {0.0, 0.0, 0.0}, gu[3] = {0.0, 0.0, 0.0};
 #pragma unroll
     for (int a = 0; a < 4; a++) {
@@ -455,6 +418,7 @@ void assemble_operator(Ctx& c, const double* coef_host, double lambda) {
     FG_CUDA(cudaMemcpyToSymbolAsync(c_tri_q, q, sizeof(q), 0, cudaMemcpyHostToDevice, s));
   }
   DBuf<double>& coef = c.coef;  // kept for the adjoint gradient
+  c.lambda_mass = lambda;
   coef.release();
   if (coef_host) {
     coef.alloc(ne, s);
@@ -507,6 +471,51 @@ void element_log_coef_gradient(Ctx& c, const double* d_lam, const double* d_u, d
   else
     FG_LAUNCH(grad2d_kernel, grid_for(M.ne, 128), 128, 0, c.stream, M.xyz.p, M.conn.p, coef, M.ne, d_lam, d_u,
               d_grad);
+}
+
+void profile_assembly(Ctx& c, int which, int reps, double* ms, double* bytes) {
+  FG_REQUIRE(c.has_mesh && c.assembled_from_mesh, FEMGPU_ERR_NOT_READY, "no operator assembled from the mesh");
+  cudaStream_t s = c.stream;
+  Mesh& M = c.mesh;
+  const int64_t ne = M.ne, nv = M.nv, nnz = c.A.nnz;
+  const int k = M.k, nup = k == 4 ? 10 : 6;
+  DBuf<double> ev((size_t)ne * nup, s), vals(nnz, s);
+  DBuf<int32_t> bad(1, s);
+  bad.zero();
+  const double* coef = c.coef.n ? c.coef.p : nullptr;
+  auto element = [&]() {
+    if (k == 4)
+      FG_LAUNCH(element3d_kernel, grid_for(ne, 128), 128, 0, s, M.xyz.p, M.conn.p,
+                M.has_labels ? M.labels.p : nullptr, coef, ne, c.lambda_mass, ev.p);
+    else
+      FG_LAUNCH(element2d_kernel, grid_for(ne, 128), 128, 0, s, M.xyz.p, M.conn.p, coef, ne, c.lambda_mass, ev.p);
+  };
+  auto gather = [&]() {
+    FG_LAUNCH(gather_rows_kernel, grid_for(nv, 128), 128, 0, s, c.A.rp.p, c.A.ci.p, M.vstart.p, M.inc.p, M.conn.p,
+              ev.p, ne, (int)nv, k, vals.p, bad.p);
+  };
+  element();
+  auto run = [&]() {
+    if (which == 6) element();
+    else gather();
+  };
+  if (which == 6)  // connectivity, coefficient and entries per element, coordinates once per vertex
+    *bytes = (double)ne * (4.0 * k + (coef ? 8.0 : 0.0) + 8.0 * nup) + 24.0 * nv;
+  else  // row offsets, columns, incidence offsets and lists, the incident elements' vertices and entries, values out
+    *bytes = 8.0 * (nv + 1) + 4.0 * nnz + 4.0 * k * ne + 4.0 * k * ne + 8.0 * nup * ne + 8.0 * nnz;
+  for (int i = 0; i < 3; i++) run();
+  cudaEvent_t e0, e1;
+  FG_CUDA(cudaEventCreate(&e0));
+  FG_CUDA(cudaEventCreate(&e1));
+  FG_CUDA(cudaEventRecord(e0, s));
+  for (int i = 0; i < reps; i++) run();
+  FG_CUDA(cudaEventRecord(e1, s));
+  FG_CUDA(cudaEventSynchronize(e1));
+  float t = 0;
+  FG_CUDA(cudaEventElapsedTime(&t, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms = t / reps;
 }
 
 void apply_dirichlet(Ctx& c, const uint8_t* mask_host) {

@@ -24,8 +24,8 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "--expt-relaxed-c
               "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", INCLUDE]
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", INCLUDE]
 
-CU_SOURCES = ["primitives.cu", "fem_assembly.cu", "amg_setup.cu", "amg_solve.cu", "capi.cu", "noalloc.cu",
-              "hierarchy_io.cu"]
+CU_SOURCES = ["primitives.cu", "fem_assembly.cu", "amg_setup.cu", "amg_solve.cu", "block_solve.cu", "capi.cu",
+              "noalloc.cu", "hierarchy_io.cu"]
 CXX_SOURCES = ["quadrature.cpp", "io.cpp", "FEMSolver.cpp"]
 
 

@@ -27,7 +27,7 @@ EXPORTS = [
     "femgpu_num_levels", "femgpu_get_level_info", "femgpu_level_get", "femgpu_vcycle", "femgpu_kernel_launches",
     "femgpu_profile_kernel", "femgpu_load_vector_device_noalloc", "femgpu_adjoint_grad",
     "femgpu_adjoint_grad_device", "femgpu_solve_multi", "femgpu_solve_multi_device", "femgpu_solve_batch",
-    "femgpu_save_hierarchy", "femgpu_load_hierarchy",
+    "femgpu_save_hierarchy", "femgpu_load_hierarchy", "femgpu_test_copy_wait_limit",
     "femgpu_read_tetgen", "femgpu_read_ply", "femgpu_read_mat_sparse", "femgpu_read_mat_array",
     "femgpu_write_mat_array", "femgpu_write_vtk",
 ]
@@ -113,6 +113,7 @@ def lib():
     L.femgpu_level_get.argtypes = [_vp, C.c_int] + [_vp] * 9
     L.femgpu_vcycle.argtypes = [_vp, _f64p, _f64p]
     L.femgpu_kernel_launches.argtypes = [_vp, _pi64]
+    L.femgpu_test_copy_wait_limit.argtypes = [_vp, C.c_int]
     L.femgpu_profile_kernel.argtypes = [_vp, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.femgpu_read_tetgen.argtypes = [C.c_char_p, C.c_char_p, _pi64, _pi64, _vp, _vp, _vp]
     L.femgpu_read_ply.argtypes = [C.c_char_p, _pi64, _pi64, _vp, _vp]
@@ -282,7 +283,13 @@ class Solver:
                     setup_ms=st.setup_ms, solve_ms=st.solve_ms, levels=st.num_levels)
 
     KERNELS = {0: "spmv_dot_sliced_kernel (FP64 outer SpMV + dot, 32-row slices)", 1: "smooth pre (level 0)",
-               2: "smooth post (level 0)", 3: "spmv_lanes R (level 0)", 4: "spmv_lanes P (level 0)"}
+               2: "smooth post sweeps alone (level 0)", 3: "spmv_lanes R (level 0)", 4: "spmv_lanes P (level 0)",
+               5: "smooth post as in the V-cycle (level 0: b - A_out x, sweeps, z, z.r)",
+               6: "element kernel (assembly)", 7: "gather_rows_kernel (assembly)"}
+
+    def test_copy_wait_limit(self, polls: int):
+        """Failure-detection testing: polls of the smoother's copy wait (negative: default)."""
+        _check(lib().femgpu_test_copy_wait_limit(self.h, int(polls)), self.h)
 
     def profile_kernel(self, which: int, reps: int = 20):
         ms, nb = C.c_double(), C.c_double()

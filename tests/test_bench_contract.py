@@ -27,7 +27,11 @@ def test_reference_arm_line():
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": "DOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
-    assert d["config"]["workload"].startswith("poisson3d_kuhn_128^3")
+    # the sample it ran is the workload it names, with the GPU arm's config keys
+    assert d["config"]["workload"] == "poisson3d_kuhn_6^3_sigma2"
+    assert set(d["config"]) == {"workload", "dofs", "free_dofs", "elements", "nnz", "precision", "tolerance", "l2"}
+    assert d["config"]["dofs"] == 7 ** 3 and d["config"]["elements"] == 6 * 6 ** 3
+    assert d["config"]["precision"] == "mixed" and d["dtype"] == "f64+f32"
 
 
 def test_reference_arm_other_ranks_print_nothing():

@@ -140,9 +140,10 @@ def test_pcg_solution_against_fp64_direct_solve(precision):
     assert true_rel <= 1.05e-8
     xs = spl.spsolve(A.tocsc(), b)  # FP64 reference solution
     err = np.linalg.norm(x - xs) / np.linalg.norm(xs)
-    assert err < 1e-5, err
+    assert err < 1e-8, err  # the oracle's own PCG reaches 1.7e-9 on this problem
     xo, sto = orc.pcg(b, tol=1e-8, max_iters=300, flexible=True)
-    assert abs(st["iterations"] - sto["iters"]) <= 2
+    assert abs(st["iterations"] - sto["iters"]) <= 1
+    assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-8
 
 
 def test_single_vcycle_solver_type_0():

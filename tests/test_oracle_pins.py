@@ -146,3 +146,87 @@ def test_oracle_operator_symmetric_and_vcycle_homogeneous():
         z = amg.vcycle(r)
         assert np.array_equal(amg.vcycle(2.0 * r), 2.0 * z)
         assert np.array_equal(amg.vcycle(0.25 * r), 0.25 * z)
+
+
+def scaled_assembly_error(rp, ci, v_lib, v_ref):
+    """max |a_lib - a_ref| / sqrt(|a_ii a_jj|) over the pattern (entries scaled by their
+    diagonal pair, so structurally near-zero couplings are measured against the row scale)."""
+    n = rp.shape[0] - 1
+    rows = np.repeat(np.arange(n), np.diff(rp))
+    diag = np.zeros(n)
+    on = ci == rows
+    diag[rows[on]] = np.abs(v_ref[on])
+    scale = np.sqrt(diag[rows] * diag[ci])
+    return float(np.max(np.abs(v_lib - v_ref) / scale))
+
+
+@pytest.mark.parametrize("case", ["poisson_32_kappa", "poisson_16_sigma2", "kuhn_mass"])
+def test_library_element_formula_matches_reference_formula(case):
+    # on Kuhn cubes of 2^k cells per edge (the configurations' meshes: exact coordinates)
+    # the fused multiply-add gradients (what the GPU assembles) agree with the reference's
+    # 4x4 cofactor inverse to 1e-13 relative to the row scale
+    rng = np.random.default_rng(5)
+    if case == "poisson_32_kappa":
+        xyz, conn, kappa, f, mask = meshes.poisson3d_problem(32, sigma=1.0)
+        kw = dict(coef=kappa, lambda_mass=0.0)
+    elif case == "poisson_16_sigma2":
+        xyz, conn, kappa, f, mask = meshes.poisson3d_problem(16, sigma=2.0, kappa_seed=4)
+        kw = dict(coef=kappa, lambda_mass=0.0)
+    else:
+        xyz, conn = meshes.kuhn_cube(8)
+        kw = dict(coef=np.exp(rng.standard_normal(conn.shape[0])), lambda_mass=2.5)
+    rp, ci = O.build_pattern(xyz.shape[0], conn)
+    v_lib = O.assemble(xyz, conn, rp, ci, **kw)
+    v_ref = O.assemble(xyz, conn, rp, ci, reference_formula=True, **kw)
+    assert scaled_assembly_error(rp, ci, v_lib, v_ref) <= 1e-13
+
+
+def exact_stiffness(p):
+    """Unit-coefficient P1 stiffness of one tetrahedron in exact rational arithmetic."""
+    from fractions import Fraction
+    P = [[Fraction(float(v)) for v in row] for row in p]
+    a, b, c = ([P[q][d] - P[0][d] for d in range(3)] for q in (1, 2, 3))
+
+    def cross(u, v):
+        return [u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2], u[0] * v[1] - u[1] * v[0]]
+
+    bc, ca, ab = cross(b, c), cross(c, a), cross(a, b)
+    det = sum(a[d] * bc[d] for d in range(3))
+    g = [None, [t / det for t in bc], [t / det for t in ca], [t / det for t in ab]]
+    g[0] = [-(g[1][d] + g[2][d] + g[3][d]) for d in range(3)]
+    vol = abs(det) / 6
+    return np.array([[float(vol * sum(g[i][d] * g[j][d] for d in range(3))) for j in range(4)] for i in range(4)])
+
+
+@pytest.mark.parametrize("mesh", ["tetVol", "CubeMesh_size256step16_correct", "jittered", "kuhn9"])
+def test_element_formulas_against_exact_arithmetic(ref_data, mesh):
+    # Where coordinates are not short binary fractions (the reference's own meshes, a
+    # jittered cube, a cube of 9 cells per edge) the two formulas differ by up to a few
+    # 1e-12: the reference's cofactor inverse of [x y z 1] loses digits there, while the
+    # edge-vector gradients stay within a few units in the last place of the exact element
+    # matrix.
+    import femgpu
+    if mesh == "jittered":
+        xyz, conn = meshes.kuhn_cube(9)
+        xyz = xyz + np.random.default_rng(5).uniform(-0.03, 0.03, xyz.shape)
+    elif mesh == "kuhn9":
+        xyz, conn = meshes.kuhn_cube(9)
+    else:
+        xyz, conn, lab = femgpu.read_tetgen(os.path.join(ref_data, mesh))
+    worst_lib = worst_ref = 0.0
+    for e in np.random.default_rng(0).choice(conn.shape[0], 60, replace=False):
+        c = conn[e]
+        loc = np.arange(4, dtype=np.int32).reshape(1, 4)
+        rp, ci = O.build_pattern(4, loc)
+        Ke = exact_stiffness(xyz[c])
+        scale = np.sqrt(np.outer(np.abs(np.diag(Ke)), np.abs(np.diag(Ke))))
+        for ref, name in ((False, "lib"), (True, "ref")):
+            v = O.assemble(xyz[c], loc, rp, ci, coef=np.ones(1), lambda_mass=0.0, reference_formula=ref)
+            K = sp.csr_matrix((v, ci, rp)).toarray()
+            err = float(np.max(np.abs(K - Ke) / scale))
+            if name == "lib":
+                worst_lib = max(worst_lib, err)
+            else:
+                worst_ref = max(worst_ref, err)
+    assert worst_lib <= 2e-15, worst_lib
+    assert worst_ref >= worst_lib

@@ -13,7 +13,16 @@ from femgpu import meshes
 
 pytestmark = pytest.mark.gpu
 
-MAX_ELEMENTS = 2097152  # FEMGPU_NOALLOC_MAX_ELEMENTS in include/femgpu.h
+def _header_limit():
+    """FEMGPU_NOALLOC_MAX_ELEMENTS as include/femgpu.h defines it."""
+    import os
+    import re
+    path = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "femgpu.h")
+    with open(path) as fh:
+        return int(re.search(r"#define\s+FEMGPU_NOALLOC_MAX_ELEMENTS\s+(\d+)", fh.read()).group(1))
+
+
+MAX_ELEMENTS = _header_limit()
 
 # CUmemPool_attribute values from cuda.h
 _USED_MEM_CURRENT = 7
@@ -113,8 +122,11 @@ def test_rejects_bad_calls_without_launching():
     launches1 = femgpu.kernel_launches()
     assert s2.load_vector_device_noalloc(0, buf.data_ptr(), check=False) == 1
     assert femgpu.kernel_launches() == launches1
-    # more elements than the fixed scratch holds: 6 * 71^3 = 2,147,466 tetrahedra
-    xyz, conn = meshes.kuhn_cube(71)
+    # more elements than the fixed scratch holds: the smallest Kuhn cube above the limit
+    cells = 1
+    while 6 * cells ** 3 <= MAX_ELEMENTS:
+        cells += 1
+    xyz, conn = meshes.kuhn_cube(cells)
     assert conn.shape[0] > MAX_ELEMENTS
     big = femgpu.Solver()
     big.set_mesh(xyz, conn)
