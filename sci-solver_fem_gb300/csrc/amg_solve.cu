@@ -439,33 +439,66 @@ __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
     const int rs = grows[g], re = grows[g + 1];
     const int wb = rs + (t & ~31);  // first row of this warp's 32-row block
     const bool live = rs + t < re;
-    const int row = live ? wb + jrow[rs + t] : rs;
-    const int loc = row - rs;
-    int e0 = 0, len = 0;
-    T d = (T)1, di = (T)1, bb = (T)0, x = (T)0;
-    double dr = 0.0, dor = 0.0;  // the dot operands, loaded now so the sweeps hide their latency
+    // Every per-row input is loaded in the block's natural order (lane p loads row wb + p,
+    // no dependence on the row order), then lane p takes the values of its sorted row
+    // wb + jrow from the lane that loaded them: one memory round trip per group.
+    const int nrow = rs + t;
+    int jr = 0, ne0 = 0, ne1 = 0;
+    T nd = (T)1, ndi = (T)1, nb = (T)0, nx = (T)0;
+    double ndr = 0.0, ndor = 0.0;
     if (live) {
-      e0 = irp[row];
-      len = irp[row + 1] - e0;
-      d = diag[row];
-      di = dinv[row];
+      jr = jrow[nrow];
+      ne0 = irp[nrow];
+      ne1 = irp[nrow + 1];
+      nd = diag[nrow];
+      ndi = dinv[nrow];
       if (POST && dot_part) {
-        dr = dot_r[row];
-        if (dot_o) dor = dot_o[row];
+        ndr = dot_r[nrow];
+        if (dot_o) ndor = dot_o[nrow];
       }
       if (POST) {
-        bb = b[row];
-        if (orp) bb = gather_row<T, 8, true>(oci, ov, x_in, orp[row], orp[row + 1], 1, bb);
-        x = x_in[row];
+        nb = b[nrow];
+        if (orp) nb = gather_row<T, 8, true>(oci, ov, x_in, orp[nrow], orp[nrow + 1], 1, nb);
+        nx = x_in[nrow];
+      } else if (b64) {
+        nb = (T)b64[nrow];
+        b_store[nrow] = nb;
       } else {
-        if (b64) {
-          bb = (T)b64[row];
-          b_store[row] = bb;
-        } else {
-          bb = b[row];
-        }
-        x = (w * bb) * di;
+        nb = b[nrow];
       }
+    }
+    // the next group's per-row inputs into L2 while this group is smoothed
+    if (gn < ngroups) {
+      const int nr2 = grows[gn] + t;
+      if (nr2 < grows[gn + 1]) {
+        prefetch_l2(jrow + nr2);
+        prefetch_l2(irp + nr2);
+        prefetch_l2(diag + nr2);
+        prefetch_l2(dinv + nr2);
+        if (POST) {
+          prefetch_l2(b + nr2);
+          prefetch_l2(x_in + nr2);
+          if (orp) prefetch_l2(orp + nr2);
+          if (dot_part) {
+            prefetch_l2(dot_r + nr2);
+            if (dot_o) prefetch_l2(dot_o + nr2);
+          }
+        } else if (b64) {
+          prefetch_l2(b64 + nr2);
+        } else {
+          prefetch_l2(b + nr2);
+        }
+      }
+    }
+    const int row = wb + jr;
+    const int loc = row - rs;
+    const int e0 = __shfl_sync(0xffffffffu, ne0, jr);
+    const int len = live ? __shfl_sync(0xffffffffu, ne1, jr) - e0 : 0;
+    const T d = __shfl_sync(0xffffffffu, nd, jr), di = __shfl_sync(0xffffffffu, ndi, jr);
+    const T bb = __shfl_sync(0xffffffffu, nb, jr);
+    const double dr = __shfl_sync(0xffffffffu, ndr, jr), dor = __shfl_sync(0xffffffffu, ndor, jr);
+    T x = POST ? __shfl_sync(0xffffffffu, nx, jr) : (w * bb) * di;
+    if (live) {
 #pragma unroll
       for (int c = 0; c < kXCopies; c++) xa[loc + c * CS] = x;
     }

@@ -207,6 +207,11 @@ __host__ __device__ inline int next_pow2(int v) {
   return p;
 }
 
+// A hint to bring the line holding p into L2 (p must point into an allocation).
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 // ---- bulk asynchronous copies (TMA, 1-D) with an mbarrier -----------------------
 // cp.async.bulk moves a contiguous global range into shared memory; source,
 // destination and size must be multiples of 16 bytes.  Completion is counted in

@@ -38,7 +38,11 @@ struct Mesh {
   DBuf<int32_t> labels;   // ne
   DBuf<int32_t> vstart;   // nv + 1: incidence offsets
   DBuf<int32_t> inc;      // ne * k: e * k + a, sorted per vertex
+  // slot[q * k + b]: position, within the row of incidence q's vertex, of the column of
+  // vertex b of q's element (rows of at most kSlotRowMax entries; empty otherwise)
+  DBuf<uint8_t> slot;
 };
+constexpr int kSlotRowMax = 32;
 
 template <class T>
 struct Level {

@@ -208,6 +208,51 @@ __global__ void element2d_kernel(const double* __restrict__ xyz, const int32_t* 
   }
 }
 
+// Positions within its row of every (incidence, element vertex) pair, for the gather
+// below (one binary search each, once per mesh).
+__global__ void slot_map_kernel(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ cols,
+                                const int32_t* __restrict__ vstart, const int32_t* __restrict__ inc,
+                                const int32_t* __restrict__ conn, int nv, int k, uint8_t* __restrict__ slot,
+                                int32_t* bad) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) {
+    const int rb = rowptr[v], re = rowptr[v + 1];
+    for (int q = vstart[v]; q < vstart[v + 1]; q++) {
+      const int e = inc[q] / k;
+      for (int b = 0; b < k; b++) {
+        const int col = conn[(int64_t)e * k + b];
+        const int s = lower_bound_i32(cols, rb, re, col);
+        if (s >= re || cols[s] != col) {
+          atomicExch(bad, 1);
+          slot[(int64_t)q * k + b] = 0;
+          continue;
+        }
+        slot[(int64_t)q * k + b] = (uint8_t)(s - rb);
+      }
+    }
+  }
+}
+
+// One thread per row with its row's sums in shared memory (at most kSlotRowMax entries,
+// kSlotRowMax + 1 doubles apart per thread): the incident elements' contributions added
+// in element order at the positions the slot map gives, then the row written out.
+__global__ void gather_rows_slot_kernel(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ vstart,
+                                        const int32_t* __restrict__ inc, const uint8_t* __restrict__ slot,
+                                        const double* __restrict__ ev, int64_t ne, int nv, int k,
+                                        double* __restrict__ vals) {
+  extern __shared__ double acc_all[];
+  double* acc = acc_all + threadIdx.x * (kSlotRowMax + 1);
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) {
+    const int rb = rowptr[v], len = rowptr[v + 1] - rb;
+    for (int s = 0; s < len; s++) acc[s] = 0.0;
+    for (int q = vstart[v]; q < vstart[v + 1]; q++) {
+      const int code = inc[q];
+      const int e = code / k, a = code - e * k;
+      for (int b = 0; b < k; b++) acc[slot[(int64_t)q * k + b]] += ev[(int64_t)upper_index(a, b, k) * ne + e];
+    }
+    for (int s = 0; s < len; s++) vals[rb + s] = acc[s];
+  }
+}
+
 // One thread per row: contributions of the incident elements, in element order.
 __global__ void gather_rows_kernel(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ cols,
                                    const int32_t* __restrict__ vstart, const int32_t* __restrict__ inc,
@@ -351,6 +396,35 @@ __global__ void mask_rows_kernel(int n, const uint8_t* __restrict__ mask, const 
   if (i < n) out[i] = (mask && mask[i]) ? 0.0 : in[i];
 }
 
+__global__ void row_length_kernel(const int32_t* rowptr, int n, int32_t* len) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) len[i] = rowptr[i + 1] - rowptr[i];
+}
+
+// Longest row of the level-0 pattern.
+int reduce_max_row_length(Ctx& c) {
+  DBuf<int32_t> len(c.A.n > 0 ? c.A.n : 1, c.stream);
+  FG_LAUNCH(row_length_kernel, grid_for(c.A.n, 256), 256, 0, c.stream, c.A.rp.p, c.A.n, len.p);
+  return reduce_max(len.p, c.A.n, c.stream);
+}
+
+// Row gather of the element entries into the operator's values (slot map when built).
+void gather_rows(Ctx& c, const double* ev, double* vals) {
+  cudaStream_t s = c.stream;
+  Mesh& M = c.mesh;
+  if (M.slot.n) {
+    const size_t smem = (size_t)128 * (kSlotRowMax + 1) * sizeof(double);
+    FG_LAUNCH(gather_rows_slot_kernel, grid_for(M.nv, 128), 128, smem, s, c.A.rp.p, M.vstart.p, M.inc.p, M.slot.p,
+              ev, M.ne, (int)M.nv, M.k, vals);
+    return;
+  }
+  DBuf<int32_t> bad(1, s);
+  bad.zero();
+  FG_LAUNCH(gather_rows_kernel, grid_for(M.nv, 128), 128, 0, s, c.A.rp.p, c.A.ci.p, M.vstart.p, M.inc.p, M.conn.p,
+            ev, M.ne, (int)M.nv, M.k, vals, bad.p);
+  FG_REQUIRE(read_scalar(bad.p, s) == 0, FEMGPU_ERR_INVALID, "element entry outside the pattern");
+}
+
 }  // namespace
 
 void build_mesh_pattern(Ctx& c) {
@@ -389,6 +463,16 @@ void build_mesh_pattern(Ctx& c) {
   c.A.v.alloc(nnz, s);
   c.A.v.zero();
   FG_LAUNCH(compact_rows_kernel, grid_for((int64_t)nv * 32, 256), 256, 0, s, cand.p, coff.p, c.A.rp.p, nv, c.A.ci.p);
+  // slot map for the assembly's row gather, when every row fits its shared-memory sums
+  M.slot.release();
+  if (reduce_max_row_length(c) <= kSlotRowMax) {
+    M.slot.alloc((size_t)nslots * k, s);
+    DBuf<int32_t> bad2(1, s);
+    bad2.zero();
+    FG_LAUNCH(slot_map_kernel, grid_for(nv, 128), 128, 0, s, c.A.rp.p, c.A.ci.p, M.vstart.p, M.inc.p, M.conn.p, nv,
+              k, M.slot.p, bad2.p);
+    FG_REQUIRE(read_scalar(bad2.p, s) == 0, FEMGPU_ERR_INVALID, "element vertex outside the pattern");
+  }
   // level-0 aggregation graph: the pattern without self loops
   c.gxadj.alloc(nv + 1, s);
   c.gadj.alloc(nnz - nv > 0 ? nnz - nv : 1, s);
@@ -430,11 +514,7 @@ void assemble_operator(Ctx& c, const double* coef_host, double lambda) {
               coef.p, ne, lambda, ev.p);
   else
     FG_LAUNCH(element2d_kernel, grid_for(ne, 128), 128, 0, s, M.xyz.p, M.conn.p, coef.p, ne, lambda, ev.p);
-  DBuf<int32_t> bad(1, s);
-  bad.zero();
-  FG_LAUNCH(gather_rows_kernel, grid_for(M.nv, 128), 128, 0, s, c.A.rp.p, c.A.ci.p, M.vstart.p, M.inc.p, M.conn.p,
-            ev.p, ne, (int)M.nv, k, c.A.v.p, bad.p);
-  FG_REQUIRE(read_scalar(bad.p, s) == 0, FEMGPU_ERR_INVALID, "element entry outside the pattern");
+  gather_rows(c, ev.p, c.A.v.p);
 }
 
 void load_vector(Ctx& c, const double* f_host, double* b_host) {
@@ -480,8 +560,6 @@ void profile_assembly(Ctx& c, int which, int reps, double* ms, double* bytes) {
   const int64_t ne = M.ne, nv = M.nv, nnz = c.A.nnz;
   const int k = M.k, nup = k == 4 ? 10 : 6;
   DBuf<double> ev((size_t)ne * nup, s), vals(nnz, s);
-  DBuf<int32_t> bad(1, s);
-  bad.zero();
   const double* coef = c.coef.n ? c.coef.p : nullptr;
   auto element = [&]() {
     if (k == 4)
@@ -490,10 +568,7 @@ void profile_assembly(Ctx& c, int which, int reps, double* ms, double* bytes) {
     else
       FG_LAUNCH(element2d_kernel, grid_for(ne, 128), 128, 0, s, M.xyz.p, M.conn.p, coef, ne, c.lambda_mass, ev.p);
   };
-  auto gather = [&]() {
-    FG_LAUNCH(gather_rows_kernel, grid_for(nv, 128), 128, 0, s, c.A.rp.p, c.A.ci.p, M.vstart.p, M.inc.p, M.conn.p,
-              ev.p, ne, (int)nv, k, vals.p, bad.p);
-  };
+  auto gather = [&]() { gather_rows(c, ev.p, vals.p); };
   element();
   auto run = [&]() {
     if (which == 6) element();
@@ -501,6 +576,8 @@ void profile_assembly(Ctx& c, int which, int reps, double* ms, double* bytes) {
   };
   if (which == 6)  // connectivity, coefficient and entries per element, coordinates once per vertex
     *bytes = (double)ne * (4.0 * k + (coef ? 8.0 : 0.0) + 8.0 * nup) + 24.0 * nv;
+  else if (M.slot.n)  // row and incidence offsets, incidence lists, slot map, element entries, values out
+    *bytes = 8.0 * (nv + 1) + 4.0 * k * ne + 1.0 * k * k * ne + 8.0 * nup * ne + 8.0 * nnz;
   else  // row offsets, columns, incidence offsets and lists, the incident elements' vertices and entries, values out
     *bytes = 8.0 * (nv + 1) + 4.0 * nnz + 4.0 * k * ne + 4.0 * k * ne + 8.0 * nup * ne + 8.0 * nnz;
   for (int i = 0; i < 3; i++) run();
