@@ -55,7 +55,10 @@ typedef struct {
   int aggregatorType;       /* aggregatorType_     0 (OldMIS; others rejected) */
   int convergeType;         /* convergeType_       0 (the PCG test is relative, as in the reference) */
   double tolerance;         /* tolerance_          1e-6 */
-  int cycleType;            /* cycleType_          0 (V) */
+  int cycleType;            /* cycleType_          0 (V); 1 (W) and 2 (F) visit the next coarser
+                               level twice (W: W then W, F: W then V, the visit patterns of the
+                               reference's W_Cycle / F_Cycle), the second visit correcting the
+                               first with the coarse residual */
   int solverType;           /* solverType_         0 = one V-cycle, 1 = PCG */
   double smootherWeight;    /* smootherWeight_     1.0 */
   double proOmega;          /* proOmega_           0.67 */
@@ -155,7 +158,8 @@ femgpu_status femgpu_solve(femgpu_handle h, const double* b, double* x, femgpu_s
  * the columns are solved eight at a time: each column runs its own flexible PCG, the
  * eight in lockstep, and every operator and V-cycle application works on the n x 8 block
  * at once (sparse matrix times block), so the operators are read once per eight columns;
- * a column stops when it reaches the tolerance.  stats: summed iterations, largest
+ * a column stops when it reaches the tolerance (W and F cycles, and solverType 0, solve
+ * the columns one at a time).  stats: summed iterations, largest
  * relative residual, total solve time; the first failing column's status is returned.
  * No reference counterpart (the reference solves one right-hand side per
  * FEMSolver::solveFEM). */

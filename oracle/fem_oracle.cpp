@@ -1340,10 +1340,47 @@ void spmv_rows(const Csr<T>& A, const std::vector<T>& x, std::vector<T>& y) {
   }
 }
 
+/* Coarse visits of a cycle of type `type` (0 V, 1 W, 2 F) at a non-coarsest level: the
+ * first visit has type V for a V-cycle and W otherwise; W- and F-cycles visit a
+ * non-coarsest next level a second time (W: a W-cycle, F: a V-cycle), as the reference's
+ * W_Cycle / F_Cycle classes do (cycles/wcycle.h, cycles/fcycle.h; AMG_Level::cycle,
+ * amg_level.cu:51, never reaches them).  The second visit corrects the first:
+ * xc += cycle(bc - A_c xc), the residual formed row by row in the permuted coarse
+ * operator's entry order with separately rounded products, as the device does. */
+inline int first_visit(int type) { return type == 0 ? 0 : 1; }
+inline int second_visit(int type) { return type == 1 ? 1 : 0; }
+
+template <class T>
+void vcycle(std::vector<Level<T>>& L, int l, const orc_config& c, int type = 0);
+
+template <class T>
+void coarse_visits(std::vector<Level<T>>& L, int l, const orc_config& c, int type) {
+  Level<T>& lv = L[l];
+  Level<T>& nx = L[l + 1];
+  nx.b = lv.bc;
+  vcycle(L, l + 1, c, first_visit(type));
+  lv.xc = nx.x;
+  if (type == 0 || nx.coarsest) return;
+  const int N = nx.n;
+  std::vector<T> bp(N), xp(N), rc(N);
+  for (int i = 0; i < N; i++) {
+    bp[i] = lv.bc[nx.iperm[i]];
+    xp[i] = lv.xc[nx.iperm[i]];
+  }
+  for (int i = 0; i < N; i++) {
+    T s = bp[i];
+    for (int e = nx.Ap.rp[i]; e < nx.Ap.rp[i + 1]; e++) s = s - nx.Ap.v[e] * xp[nx.Ap.ci[e]];
+    rc[nx.iperm[i]] = s;
+  }
+  nx.b = rc;
+  vcycle(L, l + 1, c, second_visit(type));
+  for (int i = 0; i < N; i++) lv.xc[i] = lv.xc[i] + nx.x[i];
+}
+
 /* AMG_Level::cycle (amg_level.cu:22-71).  Input L[l].b in the level's own order for
  * l > 0 (permuted in, as permutation_kernel1), already permuted for l == 0. */
 template <class T>
-void vcycle(std::vector<Level<T>>& L, int l, const orc_config& c) {
+void vcycle(std::vector<Level<T>>& L, int l, const orc_config& c, int type) {
   Level<T>& lv = L[l];
   if (lv.coarsest) { /* lv.F holds the explicit inverse */
     const int N = lv.A.n;
@@ -1366,10 +1403,7 @@ void vcycle(std::vector<Level<T>>& L, int l, const orc_config& c) {
   }
   pre_smooth(lv, c);
   spmv_rows(lv.R, lv.r, lv.bc);
-  Level<T>& nx = L[l + 1];
-  nx.b = lv.bc;
-  vcycle(L, l + 1, c);
-  lv.xc = nx.x;
+  coarse_visits(L, l, c, type);
   /* x += P xc (postPCRFullSymmetric, gauss_seidel.cu:4425-4427) */
   std::vector<T> dx(lv.n);
   spmv_rows(lv.P, lv.xc, dx);
@@ -1389,11 +1423,7 @@ void precond(std::vector<Level<T>>& L, const orc_config& c, const std::vector<do
   int n = (int)r.size();
   l0.b.resize(n);
   for (int i = 0; i < n; i++) l0.b[i] = (T)r[i];
-  if (l0.coarsest) {
-    vcycle(L, 0, c);
-  } else {
-    vcycle(L, 0, c);
-  }
+  vcycle(L, 0, c, c.cycle_type);
   for (int i = 0; i < n; i++) z[i] = (double)l0.x[i];
 }
 
@@ -1685,6 +1715,7 @@ void orc_config_default(orc_config* c) {
   c->seed = 1;
   c->fp64_hierarchy = 0;
   c->threads = 0;
+  c->cycle_type = 0;
 }
 
 orc_amg* orc_amg_setup(const orc_config* cfg, int n, const int32_t* rowptr, const int32_t* cols, const double* vals,

@@ -89,6 +89,8 @@ typedef struct {
   uint32_t seed;         /* replaces srand(time(NULL)) */
   int fp64_hierarchy;    /* 0: FP32 hierarchy (reference), 1: FP64 */
   int threads;           /* OpenMP threads for the timed baseline (0 = default) */
+  int cycle_type;        /* cycleType_ 0 = V, 1 = W, 2 = F (the reference's W_Cycle / F_Cycle
+                            visit patterns, second visits in residual-correction form) */
 } orc_config;
 
 void orc_config_default(orc_config* c);

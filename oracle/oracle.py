@@ -25,7 +25,7 @@ class OrcConfig(C.Structure):
         ("max_levels", C.c_int), ("top_size", C.c_int), ("rand_mis_params", C.c_int),
         ("partition_max", C.c_int), ("pre_inner", C.c_int), ("post_inner", C.c_int),
         ("post_relaxes", C.c_int), ("smoother_weight", C.c_double), ("pro_omega", C.c_double),
-        ("seed", C.c_uint32), ("fp64_hierarchy", C.c_int), ("threads", C.c_int),
+        ("seed", C.c_uint32), ("fp64_hierarchy", C.c_int), ("threads", C.c_int), ("cycle_type", C.c_int),
     ]
 
 

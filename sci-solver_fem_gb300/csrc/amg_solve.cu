@@ -1296,13 +1296,38 @@ void stage_mark(Ctx& c, const char* what, int l) {
   c.stage_marks->emplace_back(std::string(what) + " l" + std::to_string(l), e);
 }
 
+// r = b - M x with M's rows in their stored entry order, products rounded separately.
+template <class T>
+__global__ void residual_rows_kernel(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                     const T* __restrict__ v, const T* __restrict__ b, const T* __restrict__ x,
+                                     T* __restrict__ r) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) r[i] = gather_row<T, 8, true>(ci, v, x, rp[i], rp[i + 1], 1, b[i]);
+}
+
+template <class T>
+__global__ void add_into_kernel(int n, const T* __restrict__ d, T* __restrict__ x) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] = x[i] + d[i];
+}
+
+// Coarse visits of a cycle of type `type` (cycleType: 0 V, 1 W, 2 F) from a non-coarsest
+// level: the first visit is a V-cycle for V and a W-cycle otherwise; W- and F-cycles visit
+// a non-coarsest next level a second time (W: a W-cycle, F: a V-cycle), the visit pattern
+// of the reference's W_Cycle / F_Cycle classes (cycles/wcycle.h, cycles/fcycle.h; its
+// AMG_Level::cycle, amg_level.cu:51, always recurses with V_CYCLE and never reaches them).
+// The second visit corrects the first: xc += cycle(bc - A_c xc), the residual formed with
+// the coarse level's permuted operator (the oracle forms it the same way).
+inline int cycle_first_visit(int type) { return type == 0 ? 0 : 1; }
+inline int cycle_second_visit(int type) { return type == 1 ? 1 : 0; }
+
 // b (level order for l > 0, already permuted for l == 0) -> x (same ordering).  At
 // level 0 with z_out != nullptr the result goes to z_out in FP64 instead of x_out;
 // with r64 != nullptr, b_in is first rounded from the FP64 vector r64 (by the
 // pre-smoother when it can, which also writes the rounded copy to b_in).
 template <class T>
 void vcycle(Ctx& c, Hierarchy<T>& H, int l, T* b_in, T* x_out, double* z_out = nullptr,
-            const double* r64 = nullptr) {
+            const double* r64 = nullptr, int type = 0) {
   cudaStream_t s = c.stream;
   Level<T>& L = *H.L[l];
   const int n = L.A.n;
@@ -1322,7 +1347,14 @@ void vcycle(Ctx& c, Hierarchy<T>& H, int l, T* b_in, T* x_out, double* z_out = n
   T* xc = N.coarsest ? N.x.p : N.xo.p;
   spmv_lanes(L.R, L.r.p, bc, 0, s);
   stage_mark(c, "restrict", l);
-  vcycle(c, H, l + 1, bc, xc);
+  vcycle(c, H, l + 1, bc, xc, nullptr, nullptr, cycle_first_visit(type));
+  if (type != 0 && !N.coarsest) {
+    FG_REQUIRE(N.wr.n == (size_t)N.n && N.wd.n == (size_t)N.n, FEMGPU_ERR_INVALID, "cycle work vectors missing");
+    FG_LAUNCH(residual_rows_kernel<T>, grid_for(N.n, 256), 256, 0, s, N.n, N.Ap.rp.p, N.Ap.ci.p, N.Ap.v.p, bc, xc,
+              N.wr.p);
+    vcycle(c, H, l + 1, N.wr.p, N.wd.p, nullptr, nullptr, cycle_second_visit(type));
+    FG_LAUNCH(add_into_kernel<T>, grid_for(N.n, 256), 256, 0, s, N.n, N.wd.p, xc);
+  }
   spmv_lanes(L.P, xc, L.x.p, 1, s);
   stage_mark(c, "prolong", l);
   bool z_done = false, out_done = false;
@@ -1361,7 +1393,7 @@ void precondition(Ctx& c, Hierarchy<T>& H, const double* r, double* z) {
     vcycle(c, H, 0, b, x);
     FG_LAUNCH(cast_out_kernel<T>, grid_for(n, 256), 256, 0, s, n, x, z);
   } else {
-    vcycle(c, H, 0, b, x, z, r);  // level 0 reads r and writes z itself
+    vcycle(c, H, 0, b, x, z, r, c.cfg.cycleType);  // level 0 reads r and writes z itself
   }
 }
 
@@ -1370,8 +1402,24 @@ void precondition_any(Ctx& c, const double* r, double* z) {
   else precondition(c, static_cast<Hierarchy<float>&>(*c.H), r, z);
 }
 
+// Work vectors of the second coarse visits of W- and F-cycles (allocated before any capture).
+template <class T>
+void ensure_cycle_work(Ctx& c, Hierarchy<T>& H) {
+  if (c.cfg.cycleType == 0) return;
+  for (int l = 1; l < H.num_levels; l++) {
+    Level<T>& L = *H.L[l];
+    if (L.coarsest || L.wr.n == (size_t)L.n) continue;
+    L.wr.alloc(L.n, c.stream);
+    L.wd.alloc(L.n, c.stream);
+  }
+}
+
 void ensure_work(Ctx& c, int n) {
   cudaStream_t s = c.stream;
+  if (c.H) {
+    if (c.cfg.precision == 1) ensure_cycle_work(c, static_cast<Hierarchy<double>&>(*c.H));
+    else ensure_cycle_work(c, static_cast<Hierarchy<float>&>(*c.H));
+  }
   if (c.vb.n != (size_t)n) {
     c.vb.alloc(n, s);
     c.vx.alloc(n, s);

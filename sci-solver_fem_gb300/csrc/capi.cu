@@ -199,6 +199,11 @@ femgpu_status femgpu_create(femgpu_handle* out, const femgpu_config* cfg) {
     g_last_global_error = "device index out of range";
     return FEMGPU_ERR_INVALID;
   }
+  if (h->cfg.cycleType < 0 || h->cfg.cycleType > 2 || (h->cfg.precision != 0 && h->cfg.precision != 1)) {
+    delete h;
+    g_last_global_error = "cycleType must be 0 (V), 1 (W) or 2 (F) and precision 0 or 1";
+    return FEMGPU_ERR_INVALID;
+  }
   h->device = h->cfg.device;
   femgpu_status st = guard(h, [&] {
     if (h->cfg.stream) {
@@ -257,6 +262,7 @@ femgpu_status femgpu_set_config(femgpu_handle h, const femgpu_config* cfg) {
                    cfg->postRelaxes >= 0,
                FEMGPU_ERR_INVALID, "invalid smoother options");
     FG_REQUIRE(cfg->precision == 0 || cfg->precision == 1, FEMGPU_ERR_INVALID, "precision must be 0 or 1");
+    FG_REQUIRE(cfg->cycleType >= 0 && cfg->cycleType <= 2, FEMGPU_ERR_INVALID, "cycleType must be 0 (V), 1 (W) or 2 (F)");
     femgpu_config c = *cfg;
     c.device = h->cfg.device;
     c.stream = h->cfg.stream;
@@ -267,6 +273,7 @@ femgpu_status femgpu_set_config(femgpu_handle h, const femgpu_config* cfg) {
                    c.aggregatorType != h->cfg.aggregatorType;
     h->cfg = c;
     if (rebuild) invalidate_hierarchy(*h);
+    h->hier_gen++;  // captured solve loops hold the old options (cycle, sweeps, weights): capture again
   });
 }
 
@@ -438,8 +445,8 @@ femgpu_status femgpu_solve_multi_device(femgpu_handle h, int nrhs, const double*
     FG_CUDA(cudaEventRecord(e0, h->stream));
     int iters = 0;
     double worst = 0.0;
-    if (h->cfg.solverType == 1) {
-      // PCG: the columns eight at a time, each block in lockstep with SpMM kernels
+    if (h->cfg.solverType == 1 && h->cfg.cycleType == 0) {
+      // PCG with V-cycles: the columns eight at a time, each block in lockstep with SpMM kernels
       std::vector<int> it(nrhs);
       std::vector<double> rr(nrhs);
       std::vector<femgpu_status> stc(nrhs, FEMGPU_OK);
@@ -451,7 +458,7 @@ femgpu_status femgpu_solve_multi_device(femgpu_handle h, int nrhs, const double*
       }
     } else {
       for (int j = 0; j < nrhs; j++) {
-        // one V-cycle per column (AMG_SOLVER)
+        // one column at a time: one V-cycle per column (AMG_SOLVER), or PCG with W/F cycles
         SolveResult r = amg_solve_device(*h, d_B + j * ldb, d_X + j * ldx);
         iters += r.iterations;
         worst = std::max(worst, r.relres);

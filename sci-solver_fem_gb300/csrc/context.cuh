@@ -82,6 +82,7 @@ struct Level {
   DBuf<double> Ainv;
   // work vectors (level numbering / permuted numbering)
   DBuf<T> b, x, r, xo, t, bp;  // bp: post-smoother right-hand side
+  DBuf<T> wr, wd;              // W- and F-cycles: residual and correction of a second visit
 };
 
 // Level-0-style smoother in registers: rows of at most 16 in-partition entries and

@@ -159,6 +159,14 @@ class Solver:
         self.n = 0
         self.dim = 0
 
+    def set_config(self, **options):
+        """Changes options of this context (femgpu_set_config); the next setup / solve uses them."""
+        for k, v in options.items():
+            if not hasattr(self.cfg, k):
+                raise AttributeError(f"unknown option {k}")
+            setattr(self.cfg, k, v)
+        _check(lib().femgpu_set_config(self.h, C.byref(self.cfg)), self.h)
+
     def close(self):
         if getattr(self, "h", None):
             lib().femgpu_destroy(self.h)

@@ -224,3 +224,32 @@ def test_native_library_is_the_cuda_path():
     s, _ = gpu_operator(*meshes.kuhn_cube(4))
     assert femgpu.kernel_launches() > launches0
     assert femgpu.native_library_path().endswith("libfemgpu.so")
+
+
+@pytest.mark.parametrize("cycle,n", [(1, 40), (2, 40), (1, 64), (2, 64)])
+def test_w_and_f_cycles_match_oracle(cycle, n):
+    # W- and F-cycles: the next coarser level visited twice (second visit on the coarse
+    # residual); the cycle and the PCG against the oracle with the same cycle type
+    xyz, conn, kappa, f, mask = meshes.poisson3d_problem(n, sigma=2.0)
+    rp, ci, v, b = oracle_operator(xyz, conn, coef=kappa, lam=0.0, mask=mask, f=f)
+    gx, ga = meshes.adjacency_from_pattern(rp, ci)
+    orc = O.OracleAMG(rp, ci, v, gx, ga, seed=5, cycle_type=cycle)
+    s, gb = gpu_operator(xyz, conn, coef=kappa, lam=0.0, mask=mask, f=f, seed=5, cycleType=cycle,
+                         solverType=1, tolerance=1e-8, maxIters=300, flexibleCG=1)
+    s.setup()
+    assert s.num_levels == orc.num_levels >= 3
+    r = np.random.default_rng(0).standard_normal(rp.shape[0] - 1)
+    zg, zo = s.vcycle(r), orc.vcycle(r)
+    assert np.array_equal(zg, zo), np.abs(zg - zo).max() / np.abs(zo).max()
+    x, st = s.solve(b)
+    xo, sto = orc.pcg(b, tol=1e-8, max_iters=300, flexible=True)
+    assert st["status"] == 0 and abs(st["iterations"] - sto["iters"]) <= 1
+    assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-8
+    # the V-cycle of the same hierarchy differs: the second visits change the result
+    s.set_config(cycleType=0)
+    assert not np.array_equal(s.vcycle(r), zg)
+
+
+def test_cycle_type_is_validated():
+    with pytest.raises(femgpu.FemgpuError):
+        femgpu.Solver(cycleType=3)
