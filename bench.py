@@ -204,7 +204,7 @@ def run_meshes(args):
         free += int(xyz.shape[0] - mask.sum())
 
     def timed(threads):
-        times, iters, worst = [], 0, 0.0
+        times, iters, worst, setup_ms, solve_ms = [], 0, 0.0, 0.0, 0.0
         for step in range(args.warmup + args.steps):
             t0 = time.perf_counter()
             xs, stats, _ = femgpu.solve_batch(solvers, bs, threads=threads)
@@ -213,17 +213,21 @@ def run_meshes(args):
                 times.append(dt)
                 iters = sum(t["iterations"] for t in stats)
                 worst = max(t["relres"] for t in stats)
-        return float(np.mean(times)), iters, worst
+                setup_ms = sum(t["setup_ms"] for t in stats)
+                solve_ms = sum(t["solve_ms"] for t in stats)
+        return float(np.mean(times)), iters, worst, setup_ms, solve_ms
 
-    dt, iters, worst = timed(0)
-    dt1, _, _ = timed(1)
+    dt, iters, worst, setup_sum, solve_sum = timed(0)
+    dt1, _, _, setup1, solve1 = timed(1)
     out = {"metric": "DOF/s over a batch of independent meshes (setup + PCG to 1e-8 each)", "value": free / dt,
            "unit": "DOF/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt,
            "higher_is_better": True, "dtype": "f64+f32", "data": "synthetic",
            "config": {"workload": "poisson3d_kuhn_48_meshes_12^3..40^3", "meshes": len(solvers),
                       "cells_per_edge": [int(m) for m in sizes], "free_dofs": free,
                       "timing": "host wall clock around the synchronous batch call"},
-           "one_host_thread_ms_per_step": 1e3 * dt1, "pcg_iterations_total": iters, "relres_max": worst}
+           "one_host_thread_ms_per_step": 1e3 * dt1, "pcg_iterations_total": iters, "relres_max": worst,
+           "device_ms_summed_over_meshes": {"setup": setup_sum, "solve": solve_sum,
+                                            "setup_one_thread": setup1, "solve_one_thread": solve1}}
     print(json.dumps(out))
 
 

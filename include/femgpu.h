@@ -71,6 +71,11 @@ typedef struct {
   void* stream;             /* cudaStream_t to run on; NULL = library-owned stream */
   void* mem_pool;           /* cudaMemPool_t for device buffers; NULL = a pool owned by the handle
                                that keeps freed memory for reuse until femgpu_destroy */
+  int autotune;             /* 1 (default): at setup, time each level's result-neutral launch
+                               choices (cross-partition lanes per row, cluster smoother CTAs per
+                               group) once per device and level shape and keep the fastest; the
+                               choices are cached for the process, and in the file named by the
+                               environment variable FEMGPU_TUNE_CACHE when set.  0: fixed rules */
 } femgpu_config;
 
 typedef struct {

@@ -2298,6 +2298,7 @@ void build_levels(Ctx& c, Hierarchy<T>& H) {
     L.xo.alloc(N, s);
     L.t.alloc(N, s);
     L.bp.alloc(N, s);
+    autotune_level(c, L);  // result-neutral launch choices, timed on this level's data
     H.L.push_back(std::move(nx));
     num_levels++;
   }

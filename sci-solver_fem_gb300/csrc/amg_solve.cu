@@ -18,6 +18,10 @@
 // two-stage with a fixed grid, so results are bitwise reproducible.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <map>
+#include <mutex>
+#include <string>
 
 #include <cooperative_groups.h>
 
@@ -1141,6 +1145,7 @@ __global__ void aout_lanes_kernel(int n, const int32_t* __restrict__ orp, const 
 // per row on average, else a power of two near a quarter of the average row.
 template <class T>
 int aout_lanes(const Level<T>& L) {
+  if (L.aout_lanes_tuned > 0) return L.aout_lanes_tuned;  // chosen by the autotuner (same sums)
   const double avg = L.n > 0 ? (double)L.Aout.nnz / L.n : 0.0;
   if (avg < 8.0) return 1;
   int s = 2;
@@ -1448,6 +1453,45 @@ void check_kernel_error(Ctx& c) {
 
 }  // namespace
 
+// The register-resident cluster smoother with C CTAs per group: sets the plan and returns
+// true when both its pre and post kernels have a resident configuration.
+template <class T>
+bool creg_plan(Ctx& c, Level<T>& L, int S, int K, int C) {
+  const int mcap = L.max_group_rows;
+  const int scap = (mcap + C - 1) / C;
+  const int thr = (int)std::max<int64_t>(32, ((int64_t)scap * S + 31) / 32 * 32);
+  if (thr > 1024) return false;
+  const size_t sm = 2 * (size_t)(mcap + 1) * sizeof(T);
+  for (int post = 0; post < 2; post++) {
+    CregSmoothFn<T> k = pick_creg_kernel<T>(post != 0, S, K);
+    if (sm > 48 * 1024) ensure_smem(k, sm);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(L.ngroups * C));
+    cfg.blockDim = dim3((unsigned)thr);
+    cfg.dynamicSmemBytes = sm;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)C;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    const cudaError_t e = cudaOccupancyMaxActiveClusters(&clusters, k, &cfg);
+    if (e != cudaSuccess) (void)cudaGetLastError();
+    if (e != cudaSuccess || clusters <= 0) return false;
+  }
+  L.smooth_lanes = S;
+  L.smooth_k = K;
+  L.cluster = C;
+  L.slice_rows = scap;
+  L.slice_ents = 0;
+  L.smooth_staged = false;
+  L.smooth_smem = sm;
+  L.smooth_threads = thr;
+  return true;
+}
+
 template <class T>
 void plan_smoother(Ctx& c, Level<T>& L) {
   cudaStream_t s = c.stream;
@@ -1483,41 +1527,8 @@ void plan_smoother(Ctx& c, Level<T>& L) {
   const int creg_c = (mcap + rows_per_cta - 1) / rows_per_cta;
   if (per_lane <= kLaneEntries && creg_c <= kMaxCluster && mcap < 65535) {
     const int K = per_lane <= 8 ? 8 : 16;
-    for (int C = std::max(1, creg_c); C <= kMaxCluster; C++) {
-      const int scap = (mcap + C - 1) / C;
-      const int thr = (int)std::max<int64_t>(32, ((int64_t)scap * S + 31) / 32 * 32);
-      const size_t sm = 2 * (size_t)(mcap + 1) * sizeof(T);
-      bool fits = true;
-      for (int post = 0; post < 2 && fits; post++) {
-        CregSmoothFn<T> k = pick_creg_kernel<T>(post != 0, S, K);
-        if (sm > 48 * 1024) ensure_smem(k, sm);
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3((unsigned)(L.ngroups * C));
-        cfg.blockDim = dim3((unsigned)thr);
-        cfg.dynamicSmemBytes = sm;
-        cudaLaunchAttribute at[1];
-        at[0].id = cudaLaunchAttributeClusterDimension;
-        at[0].val.clusterDim.x = (unsigned)C;
-        at[0].val.clusterDim.y = 1;
-        at[0].val.clusterDim.z = 1;
-        cfg.attrs = at;
-        cfg.numAttrs = 1;
-        int clusters = 0;
-        const cudaError_t e = cudaOccupancyMaxActiveClusters(&clusters, k, &cfg);
-        if (e != cudaSuccess) (void)cudaGetLastError();
-        fits = e == cudaSuccess && clusters > 0;
-      }
-      if (fits) {
-        L.smooth_k = K;
-        L.cluster = C;
-        L.slice_rows = scap;
-        L.slice_ents = 0;
-        L.smooth_staged = false;
-        L.smooth_smem = sm;
-        L.smooth_threads = thr;
-        return;
-      }
-    }
+    for (int C = std::max(1, creg_c); C <= kMaxCluster; C++)
+      if (creg_plan(c, L, S, K, C)) return;
   }
   int C = (int)std::min<int64_t>(kMaxCluster, ((int64_t)mcap * S + 1023) / 1024);
   if (C < 1) C = 1;
@@ -1567,6 +1578,146 @@ void plan_smoother(Ctx& c, Level<T>& L) {
 
 template void plan_smoother<float>(Ctx&, Level<float>&);
 template void plan_smoother<double>(Ctx&, Level<double>&);
+
+// ---- autotuner ---------------------------------------------------------------------------
+// Launch shapes that do not change any result are picked per level by timing the level's
+// own kernels once: the lanes per row of the cross-partition products (every lane count
+// adds the products in entry order), and the CTAs per cluster of the register-resident
+// cluster smoother (a row's sums never cross CTAs).  Choices are cached per device and
+// level shape for the life of the process, and in the file named by FEMGPU_TUNE_CACHE
+// when it is set (one "key value" per line).
+namespace {
+
+std::mutex g_tune_mu;
+std::map<std::string, int>* g_tune = nullptr;
+bool g_tune_loaded = false;
+
+std::string tune_path() {
+  const char* p = getenv("FEMGPU_TUNE_CACHE");
+  return p ? std::string(p) : std::string();
+}
+
+bool tune_lookup(const std::string& key, int* value) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  if (!g_tune) g_tune = new std::map<std::string, int>();
+  if (!g_tune_loaded) {
+    g_tune_loaded = true;
+    const std::string path = tune_path();
+    if (!path.empty()) {
+      if (FILE* f = fopen(path.c_str(), "r")) {
+        char k[512];
+        int v = 0;
+        while (fscanf(f, "%511s %d", k, &v) == 2) (*g_tune)[k] = v;
+        fclose(f);
+      }
+    }
+  }
+  auto it = g_tune->find(key);
+  if (it == g_tune->end()) return false;
+  *value = it->second;
+  return true;
+}
+
+void tune_store(const std::string& key, int value) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  if (!g_tune) g_tune = new std::map<std::string, int>();
+  (*g_tune)[key] = value;
+  const std::string path = tune_path();
+  if (!path.empty())
+    if (FILE* f = fopen(path.c_str(), "a")) {
+      fprintf(f, "%s %d\n", key.c_str(), value);
+      fclose(f);
+    }
+}
+
+std::string device_tag(int device) {
+  cudaDeviceProp p;
+  if (cudaGetDeviceProperties(&p, device) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return "dev";
+  }
+  std::string n = p.name;
+  for (char& ch : n)
+    if (ch == ' ') ch = '_';
+  return n + "_sm" + std::to_string(p.multiProcessorCount);
+}
+
+// average time of `reps` launches of fn (after one untimed launch)
+template <class F>
+float time_launches(cudaStream_t s, F&& fn, int reps = 3) {
+  fn();
+  cudaEvent_t e0, e1;
+  FG_CUDA(cudaEventCreate(&e0));
+  FG_CUDA(cudaEventCreate(&e1));
+  FG_CUDA(cudaEventRecord(e0, s));
+  for (int i = 0; i < reps; i++) fn();
+  FG_CUDA(cudaEventRecord(e1, s));
+  FG_CUDA(cudaEventSynchronize(e1));
+  float ms = 0;
+  FG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return ms / reps;
+}
+
+}  // namespace
+
+template <class T>
+void autotune_level(Ctx& c, Level<T>& L) {
+  if (!c.cfg.autotune || L.coarsest || L.n == 0) return;
+  cudaStream_t s = c.stream;
+  const std::string dev = device_tag(c.device);
+  const std::string shape = std::to_string(sizeof(T)) + "_" + std::to_string(L.n) + "_" + std::to_string(L.Ain.nnz) +
+                            "_" + std::to_string(L.Aout.nnz) + "_" + std::to_string(L.max_group_rows);
+  const bool verbose = getenv("FEMGPU_PROFILE") != nullptr;
+  // inputs of the timed launches: finite values in the level's work vectors
+  FG_CUDA(cudaMemsetAsync(L.x.p, 0, L.x.n * sizeof(T), s));
+  FG_CUDA(cudaMemsetAsync(L.r.p, 0, L.r.n * sizeof(T), s));
+  FG_CUDA(cudaMemsetAsync(L.b.p, 0, L.b.n * sizeof(T), s));
+  // cross-partition lanes
+  if (L.Aout.nnz > 0) {
+    const std::string key = dev + "|aout|" + shape;
+    int best = 0;
+    if (!tune_lookup(key, &best)) {
+      float tbest = 1e30f;
+      for (int S = 1; S <= 32; S <<= 1) {
+        L.aout_lanes_tuned = S;
+        const float t = time_launches(s, [&] { aout_residual<T>(s, L, L.x.p, L.r.p); });
+        if (t < tbest) {
+          tbest = t;
+          best = S;
+        }
+      }
+      tune_store(key, best);
+    }
+    L.aout_lanes_tuned = best;
+    if (verbose) fprintf(stderr, "[femgpu tune] level n=%d cross-partition lanes %d\n", L.n, best);
+  }
+  // CTAs per cluster of the register-resident cluster smoother
+  if (!smoother_in_registers(L.max_in_row, L.max_part_rows) && L.smooth_k > 0) {
+    const std::string key = dev + "|creg|" + shape;
+    const int S = L.smooth_lanes, K = L.smooth_k, C0 = L.cluster;
+    int best = 0;
+    if (!tune_lookup(key, &best)) {
+      float tbest = 1e30f;
+      for (int C = C0; C <= kMaxCluster; C++) {
+        if (!creg_plan(c, L, S, K, C)) continue;
+        const float t = time_launches(s, [&] { smooth_sweeps<T>(c, L, false, L.b.p, nullptr, L.x.p, L.r.p); });
+        if (t < tbest) {
+          tbest = t;
+          best = C;
+        }
+      }
+      tune_store(key, best);
+    }
+    if (best < C0 || !creg_plan(c, L, S, K, best))
+      FG_REQUIRE(creg_plan(c, L, S, K, C0), FEMGPU_ERR_LIMIT, "no resident configuration for the cluster smoother");
+    if (verbose) fprintf(stderr, "[femgpu tune] level n=%d cluster smoother CTAs per group %d\n", L.n, L.cluster);
+  }
+}
+
+template void autotune_level<float>(Ctx&, Level<float>&);
+template void autotune_level<double>(Ctx&, Level<double>&);
 
 void spmv_original(Ctx& c, const double* d_x, double* d_y) {
   FG_REQUIRE(c.has_matrix, FEMGPU_ERR_NOT_READY, "no operator");

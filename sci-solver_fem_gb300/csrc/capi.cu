@@ -162,6 +162,8 @@ void femgpu_config_default(femgpu_config* c) {
   c->precision = 0;
   c->flexibleCG = 0;
   c->stream = nullptr;
+  c->mem_pool = nullptr;
+  c->autotune = 1;
 }
 
 const char* femgpu_status_string(femgpu_status s) {

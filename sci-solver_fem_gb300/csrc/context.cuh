@@ -83,6 +83,7 @@ struct Level {
   // work vectors (level numbering / permuted numbering)
   DBuf<T> b, x, r, xo, t, bp;  // bp: post-smoother right-hand side
   DBuf<T> wr, wd;              // W- and F-cycles: residual and correction of a second visit
+  int aout_lanes_tuned = 0;    // lanes per row of the cross-partition products (0: the rule)
 };
 
 // Level-0-style smoother in registers: rows of at most 16 in-partition entries and
@@ -234,6 +235,10 @@ SolveResult amg_solve_device(Ctx& c, const double* d_b, double* d_x);
 // Chooses the smoother's launch plan for a level whose groups are built.
 template <class T>
 void plan_smoother(Ctx& c, Level<T>& L);
+// Times the level's result-neutral launch choices (cross-partition lanes, cluster size) and
+// keeps the fastest (cached per device and level shape); no-op when cfg.autotune is 0.
+template <class T>
+void autotune_level(Ctx& c, Level<T>& L);
 void amg_vcycle_device(Ctx& c, const double* d_r, double* d_z);
 void spmv_original(Ctx& c, const double* d_x, double* d_y);
 void profile_kernel(Ctx& c, int which, int reps, double* ms, double* bytes);

@@ -424,6 +424,7 @@ void load_levels(Ctx& c, Reader& r, int64_t n0) {
       L->t.alloc(L->n, c.stream);
       L->bp.alloc(L->n, c.stream);
       plan_smoother(c, *L);
+      autotune_level(c, *L);
     }
   }
   H->num_levels = nl;

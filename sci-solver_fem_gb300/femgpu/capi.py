@@ -43,6 +43,7 @@ class Config(C.Structure):
         ("blockSize", C.c_int), ("seed", C.c_uint32), ("precision", C.c_int), ("flexibleCG", C.c_int),
         ("stream", C.c_void_p),
         ("mem_pool", C.c_void_p),
+        ("autotune", C.c_int),
     ]
 
 

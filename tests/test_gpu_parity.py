@@ -253,3 +253,21 @@ def test_w_and_f_cycles_match_oracle(cycle, n):
 def test_cycle_type_is_validated():
     with pytest.raises(femgpu.FemgpuError):
         femgpu.Solver(cycleType=3)
+
+
+@pytest.mark.parametrize("n", [40, 64])
+def test_autotuned_launch_choices_keep_every_bit(n, tmp_path, monkeypatch):
+    # the autotuner only picks launch shapes that leave every sum unchanged: a tuned and an
+    # untuned handle give the same V-cycle and the same PCG iterates bit for bit
+    monkeypatch.setenv("FEMGPU_TUNE_CACHE", str(tmp_path / "tune.txt"))
+    xyz, conn, kappa, f, mask = meshes.poisson3d_problem(n, sigma=2.0)
+    runs = []
+    for tune in (1, 0):
+        s, b = gpu_operator(xyz, conn, coef=kappa, lam=0.0, mask=mask, f=f, seed=5, autotune=tune,
+                            solverType=1, tolerance=1e-8, maxIters=300, flexibleCG=1)
+        s.setup()
+        r = np.random.default_rng(0).standard_normal(s.n)
+        runs.append((s.vcycle(r), s.solve(b)))
+    (z1, (x1, st1)), (z0, (x0, st0)) = runs
+    assert np.array_equal(z1, z0)
+    assert np.array_equal(x1, x0) and st1["iterations"] == st0["iterations"]
