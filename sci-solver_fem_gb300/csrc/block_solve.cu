@@ -361,20 +361,30 @@ __device__ __forceinline__ T relax1(T x, T b, T sax, T d, T dinv, T w) {
 // Partition-block weighted Jacobi on one group of consecutive partitions per CTA (rows
 // [grows[g], grows[g + 1])), all eight columns at once: the group's x double-buffered in
 // shared memory (m x 8), the right-hand side b (pre) or b - A_out x_in (post) staged
-// beside it; in-partition entries are read from global memory (L2) once per sweep and
-// used for all columns.  Pre (POST == false): x0 = w b / d, `inner` sweeps, then x and
-// r = b - A_in x - d x.  Post: `inner` sweeps from x_in.
-template <class T, bool POST>
+// beside it.  In-partition entries are used for all eight columns: with STAGED they are
+// copied once (coalesced) into shared memory with group-local 16-bit columns, otherwise
+// they are read from global memory (L2) in every sweep.  Pre (POST == false):
+// x0 = w b / d, `inner` sweeps, then x and r = b - A_in x - d x.  Post: `inner` sweeps
+// from x_in.
+template <class T, bool POST, bool STAGED>
 __global__ void __launch_bounds__(512) blk_smooth_kernel(
     const int32_t* __restrict__ grows, const int32_t* __restrict__ irp, const int32_t* __restrict__ ici,
     const T* __restrict__ iv, const int32_t* __restrict__ orp, const int32_t* __restrict__ oci,
     const T* __restrict__ ov, const T* __restrict__ diag, const T* __restrict__ dinv, const T* __restrict__ b, T w,
-    int inner, const T* __restrict__ x_in, T* __restrict__ x_out, T* __restrict__ r_out, int mcap) {
+    int inner, const T* __restrict__ x_in, T* __restrict__ x_out, T* __restrict__ r_out, int mcap, int ecap) {
   extern __shared__ __align__(16) unsigned char sm[];
   T* xa = reinterpret_cast<T*>(sm);
   T* xb = xa + (int64_t)mcap * kBlock;
   T* sb = xb + (int64_t)mcap * kBlock;
+  T* sv = sb + (int64_t)mcap * kBlock;
+  uint16_t* sc16 = reinterpret_cast<uint16_t*>(sv + ecap);
   const int rs = grows[blockIdx.x], m = grows[blockIdx.x + 1] - rs;
+  const int es = irp[rs];
+  if (STAGED)
+    for (int q = threadIdx.x; q < irp[rs + m] - es; q += blockDim.x) {
+      sv[q] = iv[es + q];
+      sc16[q] = (uint16_t)(ici[es + q] - rs);
+    }
   for (int t = threadIdx.x; t < m; t += blockDim.x) {
     const int row = rs + t;
     V8<T> bb = ld8(b + (int64_t)row * kBlock), x0;
@@ -400,8 +410,9 @@ __global__ void __launch_bounds__(512) blk_smooth_kernel(
 #pragma unroll
     for (int j = 0; j < kBlock; j++) s.v[j] = (T)0;
     for (int e = irp[row]; e < irp[row + 1]; e++) {
-      const T a = iv[e];
-      const V8<T> xv = ld8(cur + (int64_t)(ici[e] - rs) * kBlock);
+      const T a = STAGED ? sv[e - es] : iv[e];
+      const int col = STAGED ? (int)sc16[e - es] : ici[e] - rs;
+      const V8<T> xv = ld8(cur + (int64_t)col * kBlock);
 #pragma unroll
       for (int j = 0; j < kBlock; j++) s.v[j] = fma(a, xv.v[j], s.v[j]);
     }
@@ -523,14 +534,52 @@ struct BlockState : BlockStateBase {
   DBuf<double> vb, vx, vr, vz, vp, vy, vrold, part, sc;
   DBuf<unsigned> cnt;
   double* h_sc = nullptr;
+  // the block PCG loop captured as a CUDA graph (conditional while node), per flexible flag
+  cudaGraphExec_t exec[2] = {nullptr, nullptr};
+  int64_t nodes[2] = {0, 0};
   ~BlockState() override {
+    for (cudaGraphExec_t e : exec)
+      if (e) cudaGraphExecDestroy(e);
     if (h_sc) cudaFreeHost(h_sc);
   }
 };
 
+// Continue the device-side block loop while a column is still running.
+__global__ void blk_check_kernel(const double* sc, cudaGraphConditionalHandle loop) {
+  cudaGraphSetConditional(loop, sc[G_ANY] != 0.0 ? 1u : 0u);
+}
+
+// Shared memory of blk_smooth_kernel: x twice and the right-hand side (m x 8 each), plus
+// the staged entries (values and 16-bit columns) when `ecap` > 0.
 template <class T>
-size_t blk_smooth_smem(int mcap) {
-  return (size_t)mcap * kBlock * sizeof(T) * 3;
+size_t blk_smooth_smem(int mcap, int ecap = 0) {
+  return (size_t)mcap * kBlock * sizeof(T) * 3 + (size_t)ecap * (sizeof(T) + 2);
+}
+
+// Entries are staged in shared memory when they fit beside the vectors.
+constexpr size_t kBlockStageLimit = 200 * 1024;
+template <class T>
+bool blk_staged(const Level<T>& L) {
+  return L.max_group_rows < 65536 && blk_smooth_smem<T>(L.max_group_rows, L.max_group_ents) <= kBlockStageLimit;
+}
+
+template <class T, bool POST>
+void launch_blk_smooth(cudaStream_t s, const Level<T>& L, const T* b, T w, int inner, const T* x_in, T* x_out,
+                       T* r_out) {
+  const int thr = std::min(512, std::max(32, (L.max_group_rows + 31) / 32 * 32));
+  if (blk_staged(L)) {
+    const size_t smem = blk_smooth_smem<T>(L.max_group_rows, L.max_group_ents);
+    ensure_smem(blk_smooth_kernel<T, POST, true>, smem);
+    FG_LAUNCH((blk_smooth_kernel<T, POST, true>), L.ngroups, thr, smem, s, L.grows.p, L.Ain.rp.p, L.Ain.ci.p,
+              L.Ain.v.p, L.Aout.rp.p, L.Aout.ci.p, L.Aout.v.p, L.diag.p, L.dinv.p, b, w, inner, x_in, x_out, r_out,
+              L.max_group_rows, L.max_group_ents);
+  } else {
+    const size_t smem = blk_smooth_smem<T>(L.max_group_rows);
+    ensure_smem(blk_smooth_kernel<T, POST, false>, smem);
+    FG_LAUNCH((blk_smooth_kernel<T, POST, false>), L.ngroups, thr, smem, s, L.grows.p, L.Ain.rp.p, L.Ain.ci.p,
+              L.Ain.v.p, L.Aout.rp.p, L.Aout.ci.p, L.Aout.v.p, L.diag.p, L.dinv.p, b, w, inner, x_in, x_out, r_out,
+              L.max_group_rows, 0);
+  }
 }
 
 template <class T>
@@ -544,26 +593,18 @@ void block_vcycle(Ctx& c, Hierarchy<T>& H, BlockState<T>& S, int l, T* b_in, T* 
   }
   BlockLevel<T>& W = S.lv[l];
   const T w = (T)c.cfg.smootherWeight;
-  const size_t smem = blk_smooth_smem<T>(L.max_group_rows);
-  const int thr = std::min(512, std::max(32, (L.max_group_rows + 31) / 32 * 32));
   // pre relax: x, r = b - A_in x - d x, then r -= A_out x
-  ensure_smem(blk_smooth_kernel<T, false>, smem);
-  FG_LAUNCH((blk_smooth_kernel<T, false>), L.ngroups, thr, smem, s, L.grows.p, L.Ain.rp.p, L.Ain.ci.p, L.Ain.v.p,
-            L.Aout.rp.p, L.Aout.ci.p, L.Aout.v.p, L.diag.p, L.dinv.p, b_in, w, c.cfg.preInnerIters, (const T*)nullptr,
-            W.x.p, W.r.p, L.max_group_rows);
+  launch_blk_smooth<T, false>(s, L, b_in, w, c.cfg.preInnerIters, (const T*)nullptr, W.x.p, W.r.p);
   FG_LAUNCH(blk_aout_kernel<T>, grid_for(n, 128), 128, 0, s, n, L.Aout.rp.p, L.Aout.ci.p, L.Aout.v.p, W.x.p, W.r.p);
   BlockLevel<T>& NW = S.lv[l + 1];
   FG_LAUNCH(blk_spmm_kernel<T>, grid_for(L.R.n, 128), 128, 0, s, L.R.n, L.R.rp.p, L.R.ci.p, L.R.v.p, W.r.p, NW.t.p,
             0);
   block_vcycle(c, H, S, l + 1, NW.t.p, NW.xo.p);
   FG_LAUNCH(blk_spmm_kernel<T>, grid_for(n, 128), 128, 0, s, n, L.P.rp.p, L.P.ci.p, L.P.v.p, NW.xo.p, W.x.p, 1);
-  ensure_smem(blk_smooth_kernel<T, true>, smem);
   T* src = W.x.p;
   for (int rl = 0; rl < c.cfg.postRelaxes; rl++) {
     T* dst = (rl + 1 == c.cfg.postRelaxes) ? x_out : (src == W.x.p ? W.r.p : W.x.p);
-    FG_LAUNCH((blk_smooth_kernel<T, true>), L.ngroups, thr, smem, s, L.grows.p, L.Ain.rp.p, L.Ain.ci.p, L.Ain.v.p,
-              L.Aout.rp.p, L.Aout.ci.p, L.Aout.v.p, L.diag.p, L.dinv.p, b_in, w, c.cfg.postInnerIters, src, dst,
-              (T*)nullptr, L.max_group_rows);
+    launch_blk_smooth<T, true>(s, L, b_in, w, c.cfg.postInnerIters, src, dst, (T*)nullptr);
     src = dst;
   }
   if (c.cfg.postRelaxes == 0)
@@ -664,7 +705,8 @@ void block_solve_columns(Ctx& c, Hierarchy<T>& H, int kc, const double* B, int64
   h[G_FLEX] = flexible ? 1.0 : 0.0;
   h[G_ANY] = (any && c.cfg.maxIters > 0) ? 1.0 : 0.0;
   FG_CUDA(cudaMemcpyAsync(sc, h, G_COUNT * sizeof(double), cudaMemcpyHostToDevice, s));
-  while (h[G_ANY] != 0.0) {
+  // one block PCG iteration (the last kernel decides whether another one runs)
+  auto iteration = [&]() {
     block_precondition(c, H, S, S.vr.p, S.vz.p);
     FG_LAUNCH(blk_dot_kernel, kBG, kBT, 0, s, n, S.vz.p, S.vr.p, flexible ? (const double*)S.vrold.p : nullptr, part,
               sc, (int)B_RZNEW, (int)B_ZROLD, S.cnt.p);
@@ -673,8 +715,60 @@ void block_solve_columns(Ctx& c, Hierarchy<T>& H, int kc, const double* B, int64
     FG_LAUNCH(blk_spmv_dot_kernel, kBG, kBT, 0, s, n, off, rp, ci, v, S.vp.p, S.vy.p, part, sc, S.cnt.p + 1);
     FG_LAUNCH(blk_update_kernel, kBG, kBT, 0, s, n, sc, S.vp.p, S.vy.p, S.vx.p, S.vr.p,
               flexible ? S.vrold.p : nullptr, part, S.cnt.p + 2);
-    FG_CUDA(cudaMemcpyAsync(h, sc, G_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s));
-    FG_CUDA(cudaStreamSynchronize(s));
+  };
+  if (h[G_ANY] != 0.0) {
+    // the iterations run on the device as a CUDA graph with a conditional while node,
+    // captured once per hierarchy (FEMGPU_HOST_LOOP: launched one by one from the host)
+    cudaGraphExec_t& exec = S.exec[flexible ? 1 : 0];
+    if (!exec && !getenv("FEMGPU_HOST_LOOP")) {
+      const int64_t before = g_kernel_launches.load();
+      cudaGraph_t g = nullptr;
+      bool ok = cudaGraphCreate(&g, 0) == cudaSuccess;
+      cudaGraphConditionalHandle loop;
+      cudaGraphNodeParams cp = {};
+      if (ok) ok = cudaGraphConditionalHandleCreate(&loop, g, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+      if (ok) {
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = loop;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t node;
+        ok = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp) == cudaSuccess;
+      }
+      if (ok)
+        ok = cudaStreamBeginCaptureToGraph(s, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                           cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+      if (ok) {
+        try {
+          iteration();
+          FG_LAUNCH(blk_check_kernel, 1, 1, 0, s, sc, loop);
+        } catch (...) {
+          ok = false;
+        }
+        cudaGraph_t captured = nullptr;
+        ok = cudaStreamEndCapture(s, &captured) == cudaSuccess && ok;
+      }
+      if (ok) ok = cudaGraphInstantiate(&exec, g, 0) == cudaSuccess;
+      if (!ok) {
+        (void)cudaGetLastError();
+        exec = nullptr;
+      }
+      if (g) cudaGraphDestroy(g);
+      S.nodes[flexible ? 1 : 0] = g_kernel_launches.load() - before;
+      g_kernel_launches.store(before);  // counted per iteration after each run
+    }
+    if (exec) {
+      FG_CUDA(cudaGraphLaunch(exec, s));
+      FG_CUDA(cudaMemcpyAsync(h, sc, G_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s));
+      FG_CUDA(cudaStreamSynchronize(s));
+      g_kernel_launches.fetch_add(S.nodes[flexible ? 1 : 0] * (int64_t)h[G_IT]);
+    } else {
+      while (h[G_ANY] != 0.0) {
+        iteration();
+        FG_CUDA(cudaMemcpyAsync(h, sc, G_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s));
+        FG_CUDA(cudaStreamSynchronize(s));
+      }
+    }
   }
   FG_LAUNCH(blk_out_kernel, grid_for(n, 256), 256, 0, s, n, kc, c.perm0.p, S.vx.p, X, ldx);
   for (int j = 0; j < kc; j++) {
