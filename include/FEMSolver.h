@@ -118,6 +118,7 @@ class FEMSolver {
   unsigned seed_;      // MIS seed (the reference uses time(NULL))
   int precision_;      // 0: FP32 hierarchy (reference), 1: FP64 hierarchy
   int flexibleCG_;     // 1: Polak-Ribiere beta
+  int smoother_;       // 0: partition-block Jacobi (reference), 1: l1-Jacobi
   femgpu_solve_stats lastStats_;
 
  private:

@@ -76,6 +76,11 @@ typedef struct {
                                group) once per device and level shape and keep the fastest; the
                                choices are cached for the process, and in the file named by the
                                environment variable FEMGPU_TUNE_CACHE when set.  0: fixed rules */
+  int smoother;             /* 0 (default): the reference's partition-block weighted Jacobi
+                               (gauss_seidel.cu dsType 0); 1: l1-Jacobi on every level's whole
+                               operator, x += w (b - A x) / l1 with l1_i = sum_j |a_ij|,
+                               preInnerIters / postInnerIters sweeps (a performance option:
+                               no partitions, no shared-memory groups, one pass over A per sweep) */
 } femgpu_config;
 
 typedef struct {

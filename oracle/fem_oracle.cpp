@@ -1340,6 +1340,31 @@ void spmv_rows(const Csr<T>& A, const std::vector<T>& x, std::vector<T>& y) {
   }
 }
 
+/* l1-Jacobi (smoother 1, the library's performance option): x += w (b - Ap x) / l1 with
+ * l1_i = sum_j |a_ij| in entry order; row sums with fused multiply-adds in entry order. */
+template <class T>
+T ap_row_sum(const Csr<T>& A, int i, const std::vector<T>& x) {
+  T s = 0;
+  for (int e = A.rp[i]; e < A.rp[i + 1]; e++) s = std::fma(A.v[e], x[A.ci[e]], s);
+  return s;
+}
+
+template <class T>
+void l1_sweeps(Level<T>& L, const orc_config& c, int sweeps) {
+  const T w = (T)c.smoother_weight;
+  std::vector<T> l1inv(L.n), xn(L.n);
+  for (int i = 0; i < L.n; i++) {
+    T s = 0;
+    for (int e = L.Ap.rp[i]; e < L.Ap.rp[i + 1]; e++) s = s + std::fabs(L.Ap.v[e]);
+    l1inv[i] = (T)1 / s;
+  }
+  for (int it = 0; it < sweeps; it++) {
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < L.n; i++) xn[i] = L.x[i] + (w * (L.b[i] - ap_row_sum(L.Ap, i, L.x))) * l1inv[i];
+    L.x.swap(xn);
+  }
+}
+
 /* Coarse visits of a cycle of type `type` (0 V, 1 W, 2 F) at a non-coarsest level: the
  * first visit has type V for a V-cycle and W otherwise; W- and F-cycles visit a
  * non-coarsest next level a second time (W: a W-cycle, F: a V-cycle), as the reference's
@@ -1401,14 +1426,25 @@ void vcycle(std::vector<Level<T>>& L, int l, const orc_config& c, int type) {
     for (int i = 0; i < lv.n; i++) tmp[i] = lv.b[lv.iperm[i]];
     lv.b.swap(tmp);
   }
-  pre_smooth(lv, c);
+  if (c.smoother == 1) {
+    lv.x.assign(lv.n, (T)0);
+    l1_sweeps(lv, c, c.pre_inner);
+    lv.r.resize(lv.n);
+    for (int i = 0; i < lv.n; i++) lv.r[i] = lv.b[i] - ap_row_sum(lv.Ap, i, lv.x);
+  } else {
+    pre_smooth(lv, c);
+  }
   spmv_rows(lv.R, lv.r, lv.bc);
   coarse_visits(L, l, c, type);
   /* x += P xc (postPCRFullSymmetric, gauss_seidel.cu:4425-4427) */
   std::vector<T> dx(lv.n);
   spmv_rows(lv.P, lv.xc, dx);
   for (int i = 0; i < lv.n; i++) lv.x[i] = lv.x[i] + dx[i];
-  post_smooth(lv, c);
+  if (c.smoother == 1) {
+    for (int rl = 0; rl < c.post_relaxes; rl++) l1_sweeps(lv, c, c.post_inner);
+  } else {
+    post_smooth(lv, c);
+  }
   if (l > 0) {
     std::vector<T> tmp(lv.n);
     for (int i = 0; i < lv.n; i++) tmp[lv.iperm[i]] = lv.x[i];
@@ -1716,6 +1752,7 @@ void orc_config_default(orc_config* c) {
   c->fp64_hierarchy = 0;
   c->threads = 0;
   c->cycle_type = 0;
+  c->smoother = 0;
 }
 
 orc_amg* orc_amg_setup(const orc_config* cfg, int n, const int32_t* rowptr, const int32_t* cols, const double* vals,

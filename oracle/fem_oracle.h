@@ -91,6 +91,7 @@ typedef struct {
   int threads;           /* OpenMP threads for the timed baseline (0 = default) */
   int cycle_type;        /* cycleType_ 0 = V, 1 = W, 2 = F (the reference's W_Cycle / F_Cycle
                             visit patterns, second visits in residual-correction form) */
+  int smoother;          /* 0 = partition-block Jacobi (reference), 1 = l1-Jacobi on Ap */
 } orc_config;
 
 void orc_config_default(orc_config* c);

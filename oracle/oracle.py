@@ -26,6 +26,7 @@ class OrcConfig(C.Structure):
         ("partition_max", C.c_int), ("pre_inner", C.c_int), ("post_inner", C.c_int),
         ("post_relaxes", C.c_int), ("smoother_weight", C.c_double), ("pro_omega", C.c_double),
         ("seed", C.c_uint32), ("fp64_hierarchy", C.c_int), ("threads", C.c_int), ("cycle_type", C.c_int),
+        ("smoother", C.c_int),
     ]
 
 

@@ -46,6 +46,7 @@ FEMSolver::FEMSolver(std::string fname, bool isTetMesh, bool verbose)
       seed_(1),
       precision_(0),
       flexibleCG_(0),
+      smoother_(0),
       lastStats_(),
       h_(nullptr) {
   int64_t nv = 0, ne = 0;
@@ -111,6 +112,7 @@ femgpu_config FEMSolver::config() const {
   c.seed = seed_;
   c.precision = precision_;
   c.flexibleCG = flexibleCG_;
+  c.smoother = smoother_;
   return c;
 }
 

@@ -1316,6 +1316,83 @@ __global__ void add_into_kernel(int n, const T* __restrict__ d, T* __restrict__ 
   if (i < n) x[i] = x[i] + d[i];
 }
 
+// ---- l1-Jacobi smoother (cfg.smoother == 1) ---------------------------------------------
+// A point smoother on the level's whole permuted operator Ap (Baker, Falgout, Kolev and Yang,
+// "Multigrid smoothers for ultraparallel computing", SISC 2011): x += w (b - A x) / l1 with
+// l1_i = sum_j |a_ij|, convergent for any symmetric positive definite A without a damping
+// estimate.  Row sums with fused multiply-adds in entry order (the oracle uses the same).
+template <class T>
+__global__ void l1_inverse_kernel(int n, const int32_t* __restrict__ rp, const T* __restrict__ v,
+                                  T* __restrict__ l1inv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  T s = 0;
+  for (int e = rp[i]; e < rp[i + 1]; e++) s = s + fabs(v[e]);
+  l1inv[i] = (T)1 / s;
+}
+
+template <class T>
+__device__ __forceinline__ T row_fma_sum(const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                        const T* __restrict__ v, const T* __restrict__ x, int i) {
+  const int a = rp[i], b = rp[i + 1];
+  T s = 0;
+  for (int e0 = a; e0 < b; e0 += 8) {
+    int c[8];
+    T w[8], xv[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      c[k] = e0 + k < b ? ci[e0 + k] : 0;
+      w[k] = e0 + k < b ? v[e0 + k] : (T)0;
+    }
+#pragma unroll
+    for (int k = 0; k < 8; k++) xv[k] = e0 + k < b ? x[c[k]] : (T)0;
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+      if (e0 + k < b) s = fma(w[k], xv[k], s);
+  }
+  return s;
+}
+
+// xout = xin + (w (b - A xin)) l1inv
+template <class T>
+__global__ void l1_sweep_kernel(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                const T* __restrict__ v, const T* __restrict__ b, const T* __restrict__ l1inv, T w,
+                                const T* __restrict__ xin, T* __restrict__ xout) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const T s = row_fma_sum(rp, ci, v, xin, i);
+  xout[i] = xin[i] + (w * (b[i] - s)) * l1inv[i];
+}
+
+// The first sweep from x = 0: the row sums vanish (+0), so x = 0 + (w (b - 0)) l1inv with no
+// pass over A (the same bits as the general sweep on a zero vector).
+template <class T>
+__global__ void l1_first_sweep_kernel(int n, const T* __restrict__ b, const T* __restrict__ l1inv, T w,
+                                      T* __restrict__ x) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] = (T)0 + (w * (b[i] - (T)0)) * l1inv[i];
+}
+
+// r = b - A x
+template <class T>
+__global__ void full_residual_kernel(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                     const T* __restrict__ v, const T* __restrict__ b, const T* __restrict__ x,
+                                     T* __restrict__ r) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) r[i] = b[i] - row_fma_sum(rp, ci, v, x, i);
+}
+
+// `sweeps` l1-Jacobi sweeps from L.x (ping-pong with L.r; the result is left in L.x).
+template <class T>
+void l1_sweeps(Ctx& c, Level<T>& L, const T* b, int sweeps) {
+  const T w = (T)c.cfg.smootherWeight;
+  for (int it = 0; it < sweeps; it++) {
+    FG_LAUNCH(l1_sweep_kernel<T>, grid_for(L.n, 256), 256, 0, c.stream, L.n, L.Ap.rp.p, L.Ap.ci.p, L.Ap.v.p, b,
+              L.l1inv.p, w, L.x.p, L.r.p);
+    std::swap(L.x.p, L.r.p);
+  }
+}
+
 // Coarse visits of a cycle of type `type` (cycleType: 0 V, 1 W, 2 F) from a non-coarsest
 // level: the first visit is a V-cycle for V and a W-cycle otherwise; W- and F-cycles visit
 // a non-coarsest next level a second time (W: a W-cycle, F: a V-cycle), the visit pattern
@@ -1342,10 +1419,26 @@ void vcycle(Ctx& c, Hierarchy<T>& H, int l, T* b_in, T* x_out, double* z_out = n
     return;
   }
   const T* b = b_in;  // already in this level's order (the parent's restriction writes it so)
-  smooth<T>(c, L, false, b, nullptr, L.x.p, L.r.p, r64, b_in);
-  stage_mark(c, "pre", l);
-  aout_residual<T>(s, L, L.x.p, L.r.p);
-  stage_mark(c, "residual", l);
+  const bool l1 = c.cfg.smoother == 1;
+  if (l1) {
+    // l1-Jacobi from x = 0, then r = b - A x
+    if (r64) FG_LAUNCH(cast_in_kernel<T>, grid_for(n, 256), 256, 0, s, n, r64, b_in);
+    if (c.cfg.preInnerIters > 0) {
+      FG_LAUNCH(l1_first_sweep_kernel<T>, grid_for(n, 256), 256, 0, s, n, b, L.l1inv.p, (T)c.cfg.smootherWeight,
+                L.x.p);
+      l1_sweeps(c, L, b, c.cfg.preInnerIters - 1);
+    } else {
+      FG_CUDA(cudaMemsetAsync(L.x.p, 0, (size_t)n * sizeof(T), s));
+    }
+    FG_LAUNCH(full_residual_kernel<T>, grid_for(n, 256), 256, 0, s, n, L.Ap.rp.p, L.Ap.ci.p, L.Ap.v.p, b, L.x.p,
+              L.r.p);
+    stage_mark(c, "pre", l);
+  } else {
+    smooth<T>(c, L, false, b, nullptr, L.x.p, L.r.p, r64, b_in);
+    stage_mark(c, "pre", l);
+    aout_residual<T>(s, L, L.x.p, L.r.p);
+    stage_mark(c, "residual", l);
+  }
   // next level: input in its t (or b when coarsest), output in its xo (or x)
   Level<T>& N = *H.L[l + 1];
   T* bc = N.coarsest ? N.b.p : N.t.p;
@@ -1363,7 +1456,10 @@ void vcycle(Ctx& c, Hierarchy<T>& H, int l, T* b_in, T* x_out, double* z_out = n
   spmv_lanes(L.P, xc, L.x.p, 1, s);
   stage_mark(c, "prolong", l);
   bool z_done = false, out_done = false;
-  for (int rl = 0; rl < c.cfg.postRelaxes; rl++) {
+  if (l1) {
+    for (int rl = 0; rl < c.cfg.postRelaxes; rl++) l1_sweeps(c, L, b, c.cfg.postInnerIters);
+  }
+  for (int rl = 0; rl < (l1 ? 0 : c.cfg.postRelaxes); rl++) {
     const bool last = rl + 1 == c.cfg.postRelaxes;
     // the last post relax of level 0 writes z itself; of a coarser level, x_out (this
     // level's order, which the parent's prolongation reads)
@@ -1407,9 +1503,17 @@ void precondition_any(Ctx& c, const double* r, double* z) {
   else precondition(c, static_cast<Hierarchy<float>&>(*c.H), r, z);
 }
 
-// Work vectors of the second coarse visits of W- and F-cycles (allocated before any capture).
+// Work vectors of the second coarse visits of W- and F-cycles and the l1-Jacobi scaling
+// (allocated before any capture).
 template <class T>
 void ensure_cycle_work(Ctx& c, Hierarchy<T>& H) {
+  if (c.cfg.smoother == 1)
+    for (int l = 0; l < H.num_levels; l++) {
+      Level<T>& L = *H.L[l];
+      if (L.coarsest || L.l1inv.n == (size_t)L.n) continue;
+      L.l1inv.alloc(L.n, c.stream);
+      FG_LAUNCH(l1_inverse_kernel<T>, grid_for(L.n, 256), 256, 0, c.stream, L.n, L.Ap.rp.p, L.Ap.v.p, L.l1inv.p);
+    }
   if (c.cfg.cycleType == 0) return;
   for (int l = 1; l < H.num_levels; l++) {
     Level<T>& L = *H.L[l];

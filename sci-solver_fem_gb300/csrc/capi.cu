@@ -164,6 +164,7 @@ void femgpu_config_default(femgpu_config* c) {
   c->stream = nullptr;
   c->mem_pool = nullptr;
   c->autotune = 1;
+  c->smoother = 0;
 }
 
 const char* femgpu_status_string(femgpu_status s) {
@@ -201,9 +202,10 @@ femgpu_status femgpu_create(femgpu_handle* out, const femgpu_config* cfg) {
     g_last_global_error = "device index out of range";
     return FEMGPU_ERR_INVALID;
   }
-  if (h->cfg.cycleType < 0 || h->cfg.cycleType > 2 || (h->cfg.precision != 0 && h->cfg.precision != 1)) {
+  if (h->cfg.cycleType < 0 || h->cfg.cycleType > 2 || (h->cfg.precision != 0 && h->cfg.precision != 1) ||
+      (h->cfg.smoother != 0 && h->cfg.smoother != 1)) {
     delete h;
-    g_last_global_error = "cycleType must be 0 (V), 1 (W) or 2 (F) and precision 0 or 1";
+    g_last_global_error = "cycleType must be 0 (V), 1 (W) or 2 (F), precision and smoother 0 or 1";
     return FEMGPU_ERR_INVALID;
   }
   h->device = h->cfg.device;
@@ -265,6 +267,7 @@ femgpu_status femgpu_set_config(femgpu_handle h, const femgpu_config* cfg) {
                FEMGPU_ERR_INVALID, "invalid smoother options");
     FG_REQUIRE(cfg->precision == 0 || cfg->precision == 1, FEMGPU_ERR_INVALID, "precision must be 0 or 1");
     FG_REQUIRE(cfg->cycleType >= 0 && cfg->cycleType <= 2, FEMGPU_ERR_INVALID, "cycleType must be 0 (V), 1 (W) or 2 (F)");
+    FG_REQUIRE(cfg->smoother == 0 || cfg->smoother == 1, FEMGPU_ERR_INVALID, "smoother must be 0 or 1");
     femgpu_config c = *cfg;
     c.device = h->cfg.device;
     c.stream = h->cfg.stream;
@@ -447,7 +450,7 @@ femgpu_status femgpu_solve_multi_device(femgpu_handle h, int nrhs, const double*
     FG_CUDA(cudaEventRecord(e0, h->stream));
     int iters = 0;
     double worst = 0.0;
-    if (h->cfg.solverType == 1 && h->cfg.cycleType == 0) {
+    if (h->cfg.solverType == 1 && h->cfg.cycleType == 0 && h->cfg.smoother == 0) {
       // PCG with V-cycles: the columns eight at a time, each block in lockstep with SpMM kernels
       std::vector<int> it(nrhs);
       std::vector<double> rr(nrhs);

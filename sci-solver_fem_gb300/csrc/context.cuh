@@ -84,6 +84,7 @@ struct Level {
   DBuf<T> b, x, r, xo, t, bp;  // bp: post-smoother right-hand side
   DBuf<T> wr, wd;              // W- and F-cycles: residual and correction of a second visit
   int aout_lanes_tuned = 0;    // lanes per row of the cross-partition products (0: the rule)
+  DBuf<T> l1inv;               // l1-Jacobi smoother: 1 / sum_j |a_ij| of Ap's rows
 };
 
 // Level-0-style smoother in registers: rows of at most 16 in-partition entries and

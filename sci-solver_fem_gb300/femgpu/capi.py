@@ -44,6 +44,7 @@ class Config(C.Structure):
         ("stream", C.c_void_p),
         ("mem_pool", C.c_void_p),
         ("autotune", C.c_int),
+        ("smoother", C.c_int),
     ]
 
 

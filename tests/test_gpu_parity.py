@@ -271,3 +271,25 @@ def test_autotuned_launch_choices_keep_every_bit(n, tmp_path, monkeypatch):
     (z1, (x1, st1)), (z0, (x0, st0)) = runs
     assert np.array_equal(z1, z0)
     assert np.array_equal(x1, x0) and st1["iterations"] == st0["iterations"]
+
+
+@pytest.mark.parametrize("precision,sweeps,n", [(0, 2, 40), (1, 2, 40), (0, 3, 64)])
+def test_l1_jacobi_smoother_matches_oracle(precision, sweeps, n):
+    # the performance smoother (smoother = 1): l1-Jacobi sweeps on each level's whole operator;
+    # the cycle bit for bit against the oracle's restatement, the PCG within 1e-8
+    xyz, conn, kappa, f, mask = meshes.poisson3d_problem(n, sigma=2.0)
+    rp, ci, v, b = oracle_operator(xyz, conn, coef=kappa, lam=0.0, mask=mask, f=f)
+    gx, ga = meshes.adjacency_from_pattern(rp, ci)
+    orc = O.OracleAMG(rp, ci, v, gx, ga, seed=5, smoother=1, pre_inner=sweeps, post_inner=sweeps,
+                      fp64_hierarchy=precision)
+    s, gb = gpu_operator(xyz, conn, coef=kappa, lam=0.0, mask=mask, f=f, seed=5, smoother=1, precision=precision,
+                         preInnerIters=sweeps, postInnerIters=sweeps, solverType=1, tolerance=1e-8, maxIters=300,
+                         flexibleCG=1)
+    s.setup()
+    r = np.random.default_rng(0).standard_normal(rp.shape[0] - 1)
+    zg, zo = s.vcycle(r), orc.vcycle(r)
+    assert np.array_equal(zg, zo), np.abs(zg - zo).max() / np.abs(zo).max()
+    x, st = s.solve(b)
+    xo, sto = orc.pcg(b, tol=1e-8, max_iters=300, flexible=True)
+    assert st["status"] == 0 and abs(st["iterations"] - sto["iters"]) <= 1
+    assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-8
