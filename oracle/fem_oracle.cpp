@@ -869,7 +869,27 @@ struct Level {
   bool chol = true;
   /* work vectors */
   std::vector<T> b, x, r, bc, xc, xo;
+  /* mixed precision: the FP64 values of A when its Galerkin product was formed in FP64 */
+  std::vector<double> A64v;
 };
+
+/* Mixed precision forms the Galerkin products whose result has at most
+ * kFp64GalerkinPerTop x top_size rows in FP64: the FP32 operands are widened exactly, the
+ * products and sums run in double in the usual generation order, and the result is rounded
+ * to FP32 for the level (its FP64 values feed the coarsest dense factorisation).  At the
+ * benchmark configurations these are the two coarsest levels' products. */
+constexpr int kFp64GalerkinPerTop = 32;
+
+template <class T>
+Csr<double> widen(const Csr<T>& A) {
+  Csr<double> B;
+  B.n = A.n;
+  B.m = A.m;
+  B.rp = A.rp;
+  B.ci = A.ci;
+  B.v.assign(A.v.begin(), A.v.end());
+  return B;
+}
 
 template <class T>
 Csr<T> permute(const Csr<T>& A, const std::vector<int32_t>& perm, const std::vector<int32_t>& iperm) {
@@ -1146,7 +1166,8 @@ int setup_levels(orc_amg* h, std::vector<Level<T>>& L, const Csr<double>& A, con
       lv.coarsest = true;
       lv.F.assign((size_t)N * N, 0.0);
       for (int i = 0; i < N; i++)
-        for (int e = lv.A.rp[i]; e < lv.A.rp[i + 1]; e++) lv.F[(size_t)i * N + lv.A.ci[e]] = (double)lv.A.v[e];
+        for (int e = lv.A.rp[i]; e < lv.A.rp[i + 1]; e++)
+          lv.F[(size_t)i * N + lv.A.ci[e]] = lv.A64v.empty() ? (double)lv.A.v[e] : lv.A64v[e];
       int st = dense_factor(N, lv.F, lv.piv);
       if (st) return st;
       /* explicit inverse, column j = LU solve of e_j; the coarse solve is then x = inv b */
@@ -1200,9 +1221,21 @@ int setup_levels(orc_amg* h, std::vector<Level<T>>& L, const Csr<double>& A, con
     }
     lv.P = build_prolongator(lv.Ap, lv.diag, lv.aggOf, nagg, c.pro_omega);
     lv.R = transpose(lv.P);
-    Csr<T> AP = spgemm(lv.Ap, lv.P);
     Level<T> nx;
-    nx.A = spgemm(lv.R, AP);
+    if (sizeof(T) == 4 && nagg <= kFp64GalerkinPerTop * c.top_size) {
+      const Csr<double> AP64 = spgemm(widen(lv.Ap), widen(lv.P));
+      Csr<double> A64 = spgemm(widen(lv.R), AP64);
+      nx.A.n = A64.n;
+      nx.A.m = A64.m;
+      nx.A.rp = A64.rp;
+      nx.A.ci = A64.ci;
+      nx.A.v.resize(A64.v.size());
+      for (size_t q = 0; q < A64.v.size(); q++) nx.A.v[q] = (T)A64.v[q];
+      nx.A64v.swap(A64.v);
+    } else {
+      Csr<T> AP = spgemm(lv.Ap, lv.P);
+      nx.A = spgemm(lv.R, AP);
+    }
     nx.n = nagg;
     nx.gxadj = o.xadjOut;
     nx.gadj = o.adjOut;

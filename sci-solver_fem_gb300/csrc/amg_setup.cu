@@ -1777,6 +1777,18 @@ __global__ void cast_kernel(int64_t n, const double* in, T* out) {
 }
 
 template <class T>
+__global__ void widen_kernel(int64_t n, const T* __restrict__ in, double* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (double)in[i];
+}
+
+template <class T>
+__global__ void narrow_kernel(int64_t n, const double* __restrict__ in, T* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (T)in[i];
+}
+
+template <class T>
 __global__ void densify_kernel(int n, const int32_t* rp, const int32_t* ci, const T* v, double* F) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n)
@@ -2117,7 +2129,10 @@ void build_levels(Ctx& c, Hierarchy<T>& H) {
       DBuf<int32_t> piv(N, s), st(1, s);
       F.zero();
       st.zero();
-      FG_LAUNCH(densify_kernel<T>, grid_for(N, 128), 128, 0, s, N, L.A.rp.p, L.A.ci.p, L.A.v.p, F.p);
+      if (L.A64v.n)  // formed in FP64: the dense factorisation takes those values
+        FG_LAUNCH(densify_kernel<double>, grid_for(N, 128), 128, 0, s, N, L.A.rp.p, L.A.ci.p, L.A64v.p, F.p);
+      else
+        FG_LAUNCH(densify_kernel<T>, grid_for(N, 128), 128, 0, s, N, L.A.rp.p, L.A.ci.p, L.A.v.p, F.p);
       const size_t fbytes = (size_t)N * N * sizeof(double);
       if (fbytes <= 200 * 1024) {
         if (fbytes > 48 * 1024)
@@ -2265,7 +2280,40 @@ void build_levels(Ctx& c, Hierarchy<T>& H) {
     }
     // Galerkin product A_next = R (Ap P)
     auto nx = std::make_unique<Level<T>>();
-    {
+    if (sizeof(T) == 4 && (int64_t)L.nagg <= (int64_t)kFp64GalerkinPerTop * c.cfg.topSize) {
+      // the coarse end of a mixed hierarchy: the product in FP64 on widened operands
+      DBuf<double> apv(L.Ap.nnz > 0 ? L.Ap.nnz : 1, s), pv(L.P.nnz > 0 ? L.P.nnz : 1, s),
+          rv(L.R.nnz > 0 ? L.R.nnz : 1, s);
+      FG_LAUNCH(widen_kernel<T>, grid_for(L.Ap.nnz, 256), 256, 0, s, L.Ap.nnz, L.Ap.v.p, apv.p);
+      FG_LAUNCH(widen_kernel<T>, grid_for(L.P.nnz, 256), 256, 0, s, L.P.nnz, L.P.v.p, pv.p);
+      FG_LAUNCH(widen_kernel<T>, grid_for(L.R.nnz, 256), 256, 0, s, L.R.nnz, L.R.v.p, rv.p);
+      DCsr<double> AP, A64;
+      EscArgs<double> a{};
+      a.arp = L.Ap.rp.p;
+      a.aci = L.Ap.ci.p;
+      a.av = apv.p;
+      a.brp = L.P.rp.p;
+      a.bci = L.P.ci.p;
+      a.bv = pv.p;
+      run_esc<double, ESC_SPGEMM>(c, a, N, L.nagg, AP);
+      EscArgs<double> r{};
+      r.arp = L.R.rp.p;
+      r.aci = L.R.ci.p;
+      r.av = rv.p;
+      r.brp = AP.rp.p;
+      r.bci = AP.ci.p;
+      r.bv = AP.v.p;
+      run_esc<double, ESC_SPGEMM>(c, r, L.nagg, L.nagg, A64);
+      nx->A.n = A64.n;
+      nx->A.m = A64.m;
+      nx->A.nnz = A64.nnz;
+      nx->A.rp = std::move(A64.rp);
+      nx->A.ci = std::move(A64.ci);
+      nx->A.v.alloc(A64.nnz > 0 ? A64.nnz : 1, s);
+      FG_LAUNCH(narrow_kernel<T>, grid_for(A64.nnz, 256), 256, 0, s, A64.nnz, A64.v.p, nx->A.v.p);
+      nx->A64v = std::move(A64.v);
+      pt.mark("RAP");
+    } else {
       DCsr<T> AP;
       EscArgs<T> a{};
       a.arp = L.Ap.rp.p;

@@ -85,10 +85,19 @@ struct Level {
   DBuf<T> wr, wd;              // W- and F-cycles: residual and correction of a second visit
   int aout_lanes_tuned = 0;    // lanes per row of the cross-partition products (0: the rule)
   DBuf<T> l1inv;               // l1-Jacobi smoother: 1 / sum_j |a_ij| of Ap's rows
+  // mixed precision: A's values in FP64 when its Galerkin product was formed in FP64 (the
+  // coarse end of the hierarchy); the coarsest level's dense factorisation reads them
+  DBuf<double> A64v;
 };
 
 // Level-0-style smoother in registers: rows of at most 16 in-partition entries and
 // partitions of at most 512 rows (one thread per row).
+// Mixed precision forms the Galerkin products whose result has at most
+// kFp64GalerkinPerTop x topSize rows in FP64 (FP32 operands widened exactly, products and
+// sums in double in the usual generation order, the result rounded to FP32 for the level).
+// At the benchmark configurations these are the two coarsest levels' products.
+constexpr int kFp64GalerkinPerTop = 32;
+
 constexpr int kRegRow = 16;
 constexpr int kRegGroupRows = 512;
 // The register smoother keeps kXCopies copies of the group's x in shared memory,
