@@ -128,6 +128,10 @@ femgpu_status femgpu_set_mesh(femgpu_handle h, int dim, int64_t nverts, const do
  * FEM2D.cu:358-378; perform_element_loop_2D.cuh:287-372); the reference fixes
  * lambda_mass = 1 and coef = NULL. */
 femgpu_status femgpu_assemble(femgpu_handle h, const double* coef, double lambda_mass);
+/* Same with the per-element coefficients in device memory (d_coef may be NULL); returns once
+ * the operator is assembled.  No reference counterpart (device-resident callers such as the
+ * PyTorch binding). */
+femgpu_status femgpu_assemble_device(femgpu_handle h, const double* d_coef, double lambda_mass);
 
 /* Load vector b = M f (consistent P1 mass) for nodal f (host arrays, nverts).
  * No reference counterpart: its force function is 0 (perform_element_loop_3D.cuh:22-26). */

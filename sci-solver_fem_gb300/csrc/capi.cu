@@ -325,6 +325,19 @@ femgpu_status femgpu_assemble(femgpu_handle h, const double* coef, double lambda
   });
 }
 
+femgpu_status femgpu_assemble_device(femgpu_handle h, const double* d_coef, double lambda_mass) {
+  if (!h) return FEMGPU_ERR_INVALID;
+  return guard(h, [&] {
+    FG_REQUIRE(h->has_mesh, FEMGPU_ERR_NOT_READY, "femgpu_set_mesh first");
+    invalidate_hierarchy(*h);
+    assemble_operator(*h, d_coef, lambda_mass, true);
+    h->has_matrix = true;
+    h->assembled_from_mesh = true;
+    h->dmask.release();
+    FG_CUDA(cudaStreamSynchronize(h->stream));
+  });
+}
+
 femgpu_status femgpu_load_vector(femgpu_handle h, const double* f, double* b) {
   if (!h || !f || !b) return FEMGPU_ERR_INVALID;
   return guard(h, [&] {

@@ -211,7 +211,8 @@ struct Ctx {
 
 // fem_assembly.cu
 void build_mesh_pattern(Ctx& c);
-void assemble_operator(Ctx& c, const double* coef_host, double lambda);
+// coef: per-element coefficients (host array, or device array when coef_on_device), or null
+void assemble_operator(Ctx& c, const double* coef_host, double lambda, bool coef_on_device = false);
 void load_vector(Ctx& c, const double* f_host, double* b_host);
 // The two load-vector passes on device f/b with caller-provided scratch (`scale`
 // and `fsum`, one double per element each); enqueued on c.stream, allocates nothing.

@@ -480,7 +480,7 @@ void build_mesh_pattern(Ctx& c) {
   c.graph_nnz = nnz - nv;
 }
 
-void assemble_operator(Ctx& c, const double* coef_host, double lambda) {
+void assemble_operator(Ctx& c, const double* coef_host, double lambda, bool coef_on_device) {
   cudaStream_t s = c.stream;
   Mesh& M = c.mesh;
   const int64_t ne = M.ne;
@@ -506,7 +506,10 @@ void assemble_operator(Ctx& c, const double* coef_host, double lambda) {
   coef.release();
   if (coef_host) {
     coef.alloc(ne, s);
-    coef.upload(coef_host, ne);
+    if (coef_on_device)
+      FG_CUDA(cudaMemcpyAsync(coef.p, coef_host, ne * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    else
+      coef.upload(coef_host, ne);
   }
   DBuf<double> ev((size_t)ne * nup, s);
   if (k == 4)

@@ -22,7 +22,7 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "not ready", 4: "b
 EXPORTS = [
     "femgpu_config_default", "femgpu_create", "femgpu_destroy", "femgpu_set_config", "femgpu_status_string",
     "femgpu_last_error",
-    "femgpu_set_mesh", "femgpu_assemble", "femgpu_load_vector", "femgpu_set_dirichlet", "femgpu_set_matrix_csr",
+    "femgpu_set_mesh", "femgpu_assemble", "femgpu_assemble_device", "femgpu_load_vector", "femgpu_set_dirichlet", "femgpu_set_matrix_csr",
     "femgpu_setup", "femgpu_solve", "femgpu_solve_device", "femgpu_spmv_device", "femgpu_get_matrix",
     "femgpu_num_levels", "femgpu_get_level_info", "femgpu_level_get", "femgpu_vcycle", "femgpu_kernel_launches",
     "femgpu_profile_kernel", "femgpu_load_vector_device_noalloc", "femgpu_adjoint_grad",
@@ -93,6 +93,7 @@ def lib():
     L.femgpu_last_error.restype = C.c_char_p
     L.femgpu_set_mesh.argtypes = [_vp, C.c_int, _i64, _f64p, _i64, _i32p, _vp]
     L.femgpu_assemble.argtypes = [_vp, _vp, C.c_double]
+    L.femgpu_assemble_device.argtypes = [_vp, _vp, C.c_double]
     L.femgpu_load_vector.argtypes = [_vp, _f64p, _f64p]
     L.femgpu_set_dirichlet.argtypes = [_vp, _u8p]
     L.femgpu_set_matrix_csr.argtypes = [_vp, _i64, _i32p, _i32p, _f64p]
@@ -201,6 +202,10 @@ class Solver:
     def assemble(self, coef=None, lambda_mass=1.0):
         coef = None if coef is None else np.ascontiguousarray(coef, dtype=np.float64)
         _check(lib().femgpu_assemble(self.h, _ptr(coef), float(lambda_mass)), self.h)
+
+    def assemble_device(self, coef_ptr: int, lambda_mass=0.0):
+        """Per-element coefficients in device memory (e.g. tensor.data_ptr())."""
+        _check(lib().femgpu_assemble_device(self.h, _vp(coef_ptr), float(lambda_mass)), self.h)
 
     def load_vector(self, f):
         b = np.zeros(self.n)
@@ -339,12 +344,13 @@ class Solver:
         return out, dict(status=status, iterations=st.iterations, relres=st.relative_residual,
                          solve_ms=st.solve_ms)
 
-    def adjoint_grad_device(self, dLdu_ptr: int, u_ptr: int, grad_ptr: int):
-        """Device pointers on the handle's stream."""
+    def adjoint_grad_device(self, dLdu_ptr: int, u_ptr: int, grad_ptr: int, check=False):
+        """Device pointers on the handle's stream; returns the status with the statistics."""
         st = SolveStats()
-        _check(lib().femgpu_adjoint_grad_device(self.h, _vp(dLdu_ptr), _vp(u_ptr), _vp(grad_ptr), C.byref(st)),
-               self.h)
-        return dict(iterations=st.iterations, relres=st.relative_residual, solve_ms=st.solve_ms)
+        status = lib().femgpu_adjoint_grad_device(self.h, _vp(dLdu_ptr), _vp(u_ptr), _vp(grad_ptr), C.byref(st))
+        if check and status != 0:
+            _check(status, self.h)
+        return dict(status=status, iterations=st.iterations, relres=st.relative_residual, solve_ms=st.solve_ms)
 
     def spmv_device(self, x_ptr: int, y_ptr: int):
         _check(lib().femgpu_spmv_device(self.h, _vp(x_ptr), _vp(y_ptr)), self.h)

@@ -58,22 +58,26 @@ def test_adjoint_gradient_matches_central_differences():
     assert rel <= 1e-6, rel
 
 
-def test_torch_autograd_binding():
+@pytest.mark.parametrize("device", ["cpu", "cuda"])
+def test_torch_autograd_binding(device):
+    # CUDA tensors stay on the device (device entry points), CPU tensors go through the host
     torch = pytest.importorskip("torch")
     from femgpu.autograd import fem_solve
 
     xyz, conn, theta, mask, b, S, u_obs = R.problem(8, dim=3)
     s = femgpu.Solver(solverType=1, tolerance=1e-12, maxIters=1000, flexibleCG=1, seed=3)
     s.set_mesh(xyz, conn)
-    th = torch.tensor(theta, dtype=torch.float64, requires_grad=True)
-    u = fem_solve(s, th, torch.from_numpy(b), mask=mask)
-    Si = torch.from_numpy(S)
-    loss = 0.5 * ((u[Si] - torch.from_numpy(u_obs)[Si]) ** 2).sum()
+    th = torch.tensor(theta, dtype=torch.float64, device=device, requires_grad=True)
+    u = fem_solve(s, th, torch.from_numpy(b).to(device), mask=mask)
+    assert u.device.type == device
+    Si = torch.from_numpy(S).to(device)
+    loss = 0.5 * ((u[Si] - torch.from_numpy(u_obs).to(device)[Si]) ** 2).sum()
     loss.backward()
-    u_np = u.detach().numpy()
+    assert th.grad.device.type == device
+    u_np = u.detach().cpu().numpy()
     _, dLdu = R.loss_and_dLdu(u_np, S, u_obs)
     g_ref = R.gradient(xyz, conn, theta, mask, dLdu, u_np)
-    rel = np.linalg.norm(th.grad.numpy() - g_ref) / np.linalg.norm(g_ref)
+    rel = np.linalg.norm(th.grad.cpu().numpy() - g_ref) / np.linalg.norm(g_ref)
     assert rel < 1e-8, rel
 
 
@@ -85,3 +89,15 @@ def test_adjoint_needs_mesh_assembly():
     s.set_matrix_csr(A.indptr.astype(np.int32), A.indices.astype(np.int32), A.data)
     with pytest.raises(femgpu.FemgpuError):
         s.adjoint_grad(np.ones(xyz.shape[0]), np.ones(xyz.shape[0]))
+
+
+def test_torch_binding_raises_when_the_solve_fails():
+    torch = pytest.importorskip("torch")
+    from femgpu.autograd import fem_solve
+
+    xyz, conn, theta, mask, b, S, u_obs = R.problem(8, dim=3)
+    s = femgpu.Solver(solverType=1, tolerance=1e-14, maxIters=2, flexibleCG=1, seed=3)
+    s.set_mesh(xyz, conn)
+    th = torch.tensor(theta, dtype=torch.float64, device="cuda", requires_grad=True)
+    with pytest.raises(RuntimeError, match="forward PCG"):
+        fem_solve(s, th, torch.from_numpy(b).cuda(), mask=mask)
