@@ -496,12 +496,15 @@ __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
     }
     const int row = wb + jr;
     const int loc = row - rs;
+    // every lane of the warp executes every shuffle (none sits under a lane-dependent branch)
     const int e0 = __shfl_sync(0xffffffffu, ne0, jr);
-    const int len = live ? __shfl_sync(0xffffffffu, ne1, jr) - e0 : 0;
+    const int e1 = __shfl_sync(0xffffffffu, ne1, jr);
+    const int len = live ? e1 - e0 : 0;
     const T d = __shfl_sync(0xffffffffu, nd, jr), di = __shfl_sync(0xffffffffu, ndi, jr);
     const T bb = __shfl_sync(0xffffffffu, nb, jr);
     const double dr = __shfl_sync(0xffffffffu, ndr, jr), dor = __shfl_sync(0xffffffffu, ndor, jr);
-    T x = POST ? __shfl_sync(0xffffffffu, nx, jr) : (w * bb) * di;
+    const T xs = __shfl_sync(0xffffffffu, nx, jr);
+    T x = POST ? xs : (w * bb) * di;
     if (live) {
 #pragma unroll
       for (int c = 0; c < kXCopies; c++) xa[loc + c * CS] = x;
@@ -530,7 +533,7 @@ __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
     }
     if (__syncthreads_or(!ok)) {
       if (t == 0) {
-        *kerr = 1.0;
+        *kerr = 1.0 + g;  // where: the first group whose copy did not land
         // let the copies in flight land before the CTA exits
         (void)mbar_wait_bounded(bar + buf, parity);
         if (gn < ngroups) (void)mbar_wait_bounded(bar + (buf ^ 1), (uint32_t)((i + 1) >> 1) & 1u);
@@ -1547,12 +1550,17 @@ void ensure_work(Ctx& c, int n) {
   if (!c.h_scalars) FG_CUDA(cudaMallocHost((void**)&c.h_scalars, 64 * sizeof(double)));
 }
 
+// The error slot holds 1 + the group whose staged copy a register-smoother CTA gave up on.
+std::string copy_wait_message(double v) {
+  return "smoother copy wait ran out (group " + std::to_string((long long)v - 1) + ")";
+}
+
 // Fails when a smoother CTA gave up waiting for its bulk copies (waits on the stream).
 void check_kernel_error(Ctx& c) {
   double v = 0.0;
   FG_CUDA(cudaMemcpyAsync(&v, c.red.p + 2 * kRedBlocks + S_KERR, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
   FG_CUDA(cudaStreamSynchronize(c.stream));
-  FG_REQUIRE(v == 0.0, FEMGPU_ERR_LIMIT, "smoother copy wait ran out");
+  FG_REQUIRE(v == 0.0, FEMGPU_ERR_LIMIT, copy_wait_message(v));
 }
 
 }  // namespace
@@ -2033,7 +2041,7 @@ SolveResult amg_solve_device(Ctx& c, const double* d_b, double* d_x) {
       it = (int)c.h_scalars[S_IT];
       g_kernel_launches.fetch_add(c.graph_nodes * it);
       nr = sqrt(c.h_scalars[S_NR]);
-      FG_REQUIRE(c.h_scalars[S_KERR] == 0.0, FEMGPU_ERR_LIMIT, "smoother copy wait ran out");
+      FG_REQUIRE(c.h_scalars[S_KERR] == 0.0, FEMGPU_ERR_LIMIT, copy_wait_message(c.h_scalars[S_KERR]));
       if (c.h_scalars[S_FLAG] != 0.0 || !std::isfinite(nr)) res.status = FEMGPU_ERR_BREAKDOWN;
       else if (nr / bnorm <= tol) res.status = FEMGPU_OK;
     } else {
@@ -2042,7 +2050,7 @@ SolveResult amg_solve_device(Ctx& c, const double* d_b, double* d_x) {
         FG_CUDA(cudaStreamSynchronize(s));
         it++;
         nr = sqrt(c.h_scalars[S_NR]);
-        FG_REQUIRE(c.h_scalars[S_KERR] == 0.0, FEMGPU_ERR_LIMIT, "smoother copy wait ran out");
+        FG_REQUIRE(c.h_scalars[S_KERR] == 0.0, FEMGPU_ERR_LIMIT, copy_wait_message(c.h_scalars[S_KERR]));
         if (c.h_scalars[S_FLAG] != 0.0 || !std::isfinite(nr)) {
           res.status = FEMGPU_ERR_BREAKDOWN;
           break;

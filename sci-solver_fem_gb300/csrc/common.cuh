@@ -247,12 +247,24 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return done != 0;
 }
 
-// Waits for the barrier phase with an iteration limit; false when it ran out (a limit
-// of 0 gives up without polling).
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Waits for the barrier phase with an iteration limit and a time limit; false when either
+// ran out (a limit of 0 gives up without polling).  A try_wait may suspend the thread for
+// a while before it reports an incomplete phase, so the poll count alone does not bound
+// the time: the clock is read every 64 polls and the wait ends after kMbarWaitNs.
 constexpr int kMbarWaitLimit = 1 << 22;
+constexpr uint64_t kMbarWaitNs = 500ull * 1000 * 1000;
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int limit = kMbarWaitLimit) {
-  for (int i = 0; i < limit; i++)
+  const uint64_t t0 = global_ns();
+  for (int i = 0; i < limit; i++) {
     if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 63) == 63 && global_ns() - t0 > kMbarWaitNs) return false;
+  }
   return false;
 }
 
