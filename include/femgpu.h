@@ -186,11 +186,16 @@ femgpu_status femgpu_solve_multi_device(femgpu_handle h, int nrhs, const double*
 /* Independent problems at once: for each i, femgpu_setup(h[i]) when setup != 0, then
  * femgpu_solve(h[i], b[i], x[i], &stats[i]) (host arrays, each the size of its own
  * operator).  The handles must be distinct, each with its own stream (the default;
- * handles sharing a stream are refused with FEMGPU_ERR_INVALID);
- * they run on up to `threads` host threads (0: one per handle), so the small problems'
- * setup round trips overlap and their kernels share the GPU.  Every problem is
- * attempted; the first failing status (in index order) is returned, and each failing
- * handle's femgpu_last_error names its problem.  stats may be NULL.
+ * handles sharing a stream are refused with FEMGPU_ERR_INVALID).  The setups run on up
+ * to `threads` host threads (0: one per handle), so the small problems' setup round trips
+ * overlap.  With solverType 1 on one device, the PCG solves then run as ONE CUDA graph
+ * launch: a branch per handle with its own device-side loop, so the meshes' iterations
+ * share the GPU with no host round trip; the graph is kept for the same list of handles
+ * and captured again when a hierarchy changes (stats[i].solve_ms is the whole graph's
+ * time).  Otherwise (solverType 0, FEMGPU_HOST_LOOP set, a failed setup) each solve runs on
+ * the host threads.  Every problem is attempted; the first failing status (in index
+ * order) is returned, and each failing handle's femgpu_last_error names its problem.
+ * stats may be NULL.
  * No reference counterpart (the reference solves one mesh per FEMSolver). */
 femgpu_status femgpu_solve_batch(int count, femgpu_handle* h, const double* const* b, double* const* x, int setup,
                                  int threads, femgpu_solve_stats* stats);

@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <deque>
 #include <map>
 #include <mutex>
 #include <string>
@@ -1922,13 +1923,41 @@ void pcg_iteration_body(Ctx& c, int n, int flexible, bool to_host) {
 // Captures the whole PCG loop once per hierarchy as a CUDA graph: a conditional while
 // node whose body is one iteration followed by pcg_check_kernel, so the iterations
 // run back to back on the device with no host round trip.
+// Adds to `g` a while node on `loop` after `deps` and captures its body on c.stream: one
+// PCG iteration followed by pcg_check_kernel.  Returns the node, or null when a graph call
+// or the capture failed (the capture is ended either way).
+cudaGraphNode_t add_pcg_loop(Ctx& c, int n, int flexible, cudaGraph_t g, cudaGraphConditionalHandle loop,
+                             const cudaGraphNode_t* deps, size_t ndeps) {
+  cudaStream_t s = c.stream;
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = loop;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node = nullptr;
+  if (cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &cp) != cudaSuccess) return nullptr;
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  if (cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+    return nullptr;
+  try {
+    pcg_iteration_body(c, n, flexible, false);
+    FG_LAUNCH(pcg_check_kernel, 1, 1, 0, s, c.red.p + 2 * kRedBlocks, loop);
+  } catch (...) {
+    cudaGraph_t dummy = nullptr;
+    cudaStreamEndCapture(s, &dummy);
+    return nullptr;
+  }
+  cudaGraph_t captured = nullptr;
+  if (cudaStreamEndCapture(s, &captured) != cudaSuccess) return nullptr;
+  return node;
+}
+
 bool capture_iteration(Ctx& c, int n, int flexible) {
   if (c.pcg_exec && c.graph_gen == c.hier_gen && c.graph_flexible == flexible) return true;
   if (c.pcg_exec) {
     cudaGraphExecDestroy(c.pcg_exec);
     c.pcg_exec = nullptr;
   }
-  cudaStream_t s = c.stream;
   int64_t before = g_kernel_launches.load();
   cudaGraph_t g = nullptr;
   auto fail = [&]() {
@@ -1940,26 +1969,7 @@ bool capture_iteration(Ctx& c, int n, int flexible) {
   if (cudaGraphCreate(&g, 0) != cudaSuccess) return fail();
   cudaGraphConditionalHandle loop;
   if (cudaGraphConditionalHandleCreate(&loop, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) return fail();
-  cudaGraphNodeParams cp = {};
-  cp.type = cudaGraphNodeTypeConditional;
-  cp.conditional.handle = loop;
-  cp.conditional.type = cudaGraphCondTypeWhile;
-  cp.conditional.size = 1;
-  cudaGraphNode_t node;
-  if (cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp) != cudaSuccess) return fail();
-  cudaGraph_t body = cp.conditional.phGraph_out[0];
-  if (cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
-    return fail();
-  try {
-    pcg_iteration_body(c, n, flexible, false);
-    FG_LAUNCH(pcg_check_kernel, 1, 1, 0, s, c.red.p + 2 * kRedBlocks, loop);
-  } catch (...) {
-    cudaGraph_t dummy = nullptr;
-    cudaStreamEndCapture(s, &dummy);
-    return fail();
-  }
-  cudaGraph_t captured = nullptr;
-  if (cudaStreamEndCapture(s, &captured) != cudaSuccess) return fail();
+  if (!add_pcg_loop(c, n, flexible, g, loop, nullptr, 0)) return fail();
   cudaError_t e = cudaGraphInstantiate(&c.pcg_exec, g, 0);
   cudaGraphDestroy(g);
   g = nullptr;
@@ -2066,6 +2076,196 @@ SolveResult amg_solve_device(Ctx& c, const double* d_b, double* d_x) {
   res.iterations = it;
   res.relres = nr / bnorm;
   return res;
+}
+
+// ---- the PCG solves of many meshes in one graph launch --------------------------------
+namespace {
+
+// Start of a batch branch's loop: b's norm (1 when b = 0) to S_BNORM, and the loop runs only
+// when the initial residual is above the tolerance (the host check of amg_solve_device).
+__global__ void batch_init_kernel(double* sc, cudaGraphConditionalHandle loop) {
+  double bn = sqrt(sc[S_BN]);
+  if (bn == 0.0) bn = 1.0;
+  sc[S_BNORM] = bn;
+  cudaGraphSetConditional(loop, sqrt(sc[S_NR]) / bn <= sc[S_TOL] ? 0u : 1u);
+}
+
+struct BatchGraph {
+  std::vector<Ctx*> hs;
+  std::vector<uint64_t> gens;         // each handle's hierarchy generation when captured
+  std::vector<int64_t> body_kernels;  // kernels of one iteration of each mesh's loop
+  int64_t fixed_kernels = 0;          // kernels outside the loops
+  cudaGraphExec_t exec = nullptr;
+  ~BatchGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+};
+
+std::mutex g_batch_mu;
+std::deque<std::unique_ptr<BatchGraph>> g_batch;  // most recently used first
+constexpr size_t kBatchGraphsKept = 4;
+
+// One independent branch per mesh: the kernels amg_solve_device runs before its loop (b and
+// x read from c.bat_b and c.bat_x), the PCG while loop, then x back to c.bat_x and the
+// scalars to the pinned host mirror.  Each branch is captured on its handle's stream into
+// g in three parts, since a loop body is captured on the same stream.
+bool add_batch_branch(Ctx& c, cudaGraph_t g, int64_t* body_kernels, int64_t* fixed_kernels) {
+  const int n = c.A.n;
+  cudaStream_t s = c.stream;
+  double* part = c.red.p;
+  double* sc = c.red.p + 2 * kRedBlocks;
+  const cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
+  cudaGraphConditionalHandle loop;
+  if (cudaGraphConditionalHandleCreate(&loop, g, 0, 0) != cudaSuccess) return false;
+  const int64_t k0 = g_kernel_launches.load();
+  std::vector<cudaGraphNode_t> leaves;
+  cudaGraph_t gg = nullptr;
+  if (cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0, mode) != cudaSuccess) return false;
+  bool ok = true;
+  try {
+    FG_LAUNCH(perm_vec_in_kernel, grid_for(n, 256), 256, 0, s, n, c.perm0.p, c.bat_b.p, c.vb.p);
+    FG_LAUNCH(perm_vec_in_kernel, grid_for(n, 256), 256, 0, s, n, c.perm0.p, c.bat_x.p, c.vx.p);
+    FG_LAUNCH(dot_kernel, kRedBlocks, kRedThreads, 0, s, n, c.vb.p, c.vb.p, nullptr, part, nullptr);
+    FG_LAUNCH(finalize_kernel, 1, 1024, 0, s, part, kRedBlocks, sc + S_BN);
+    launch_spmv_a0(c, n, c.vx.p, c.vy.p);
+    FG_LAUNCH(residual_kernel, kRedBlocks, kRedThreads, 0, s, n, c.vb.p, c.vy.p, c.vr.p, part);
+    FG_LAUNCH(finalize_kernel, 1, 1024, 0, s, part, kRedBlocks, sc + S_NR);
+    FG_LAUNCH(set_slot_kernel, 1, 1, 0, s, sc, S_FLAG, 0.0);
+    FG_LAUNCH(set_slot_kernel, 1, 1, 0, s, sc, S_FIRST, 1.0);
+    FG_LAUNCH(set_slot_kernel, 1, 1, 0, s, sc, S_KERR, 0.0);
+    FG_LAUNCH(set_slot_kernel, 1, 1, 0, s, sc, S_IT, 0.0);
+    FG_LAUNCH(set_slot_kernel, 1, 1, 0, s, sc, S_TOL, c.cfg.tolerance);
+    FG_LAUNCH(set_slot_kernel, 1, 1, 0, s, sc, S_MAXIT, (double)c.cfg.maxIters);
+    FG_CUDA(cudaMemsetAsync(c.rcount.p, 0, c.rcount.n * sizeof(unsigned), s));
+    FG_CUDA(cudaMemsetAsync(c.vp.p, 0, n * sizeof(double), s));
+    FG_LAUNCH(batch_init_kernel, 1, 1, 0, s, sc, loop);
+    cudaStreamCaptureStatus cs;
+    const cudaGraphNode_t* d = nullptr;
+    size_t nd = 0;
+    FG_CUDA(cudaStreamGetCaptureInfo(s, &cs, nullptr, nullptr, &d, nullptr, &nd));
+    leaves.assign(d, d + nd);
+  } catch (...) {
+    ok = false;
+  }
+  if (cudaStreamEndCapture(s, &gg) != cudaSuccess || !ok) return false;
+  const int64_t k1 = g_kernel_launches.load();
+  cudaGraphNode_t ln = add_pcg_loop(c, n, c.cfg.flexibleCG, g, loop, leaves.data(), leaves.size());
+  if (!ln) return false;
+  const int64_t k2 = g_kernel_launches.load();
+  if (cudaStreamBeginCaptureToGraph(s, g, &ln, nullptr, 1, mode) != cudaSuccess) return false;
+  try {
+    FG_LAUNCH(perm_vec_out_kernel, grid_for(n, 256), 256, 0, s, n, c.perm0.p, c.vx.p, c.bat_x.p);
+    FG_CUDA(cudaMemcpyAsync(c.h_scalars, sc, S_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s));
+  } catch (...) {
+    ok = false;
+  }
+  if (cudaStreamEndCapture(s, &gg) != cudaSuccess || !ok) return false;
+  *body_kernels = k2 - k1;
+  *fixed_kernels += (k1 - k0) + (g_kernel_launches.load() - k2);
+  return true;
+}
+
+}  // namespace
+
+void batch_prepare(Ctx& c) {
+  FG_REQUIRE(c.has_hierarchy, FEMGPU_ERR_NOT_READY, "call femgpu_setup first");
+  const int n = c.A.n;
+  ensure_work(c, n);
+  if (c.bat_b.n != (size_t)n) {
+    c.bat_b.alloc(n, c.stream);
+    c.bat_x.alloc(n, c.stream);
+  }
+}
+
+bool batch_solve_graph(const std::vector<Ctx*>& hs, std::vector<SolveResult>& res, float* ms) {
+  if (hs.empty()) return true;
+  cudaStream_t s = hs[0]->stream;
+  std::lock_guard<std::mutex> lock(g_batch_mu);
+  std::vector<uint64_t> gens(hs.size());
+  for (size_t i = 0; i < hs.size(); i++) gens[i] = hs[i]->hier_gen;
+  auto it = std::find_if(g_batch.begin(), g_batch.end(), [&](const std::unique_ptr<BatchGraph>& b) { return b->hs == hs; });
+  std::unique_ptr<BatchGraph> bg;
+  if (it != g_batch.end()) {
+    bg = std::move(*it);
+    g_batch.erase(it);
+  }
+  if (!bg || bg->gens != gens) {
+    // capture the branches again (new hierarchies, new buffers); the executable graph is
+    // updated in place when its topology is unchanged, else instantiated anew
+    const int64_t before = g_kernel_launches.load();
+    cudaGraph_t g = nullptr;
+    std::vector<int64_t> body(hs.size(), 0);
+    int64_t fixed = 0;
+    bool ok = cudaGraphCreate(&g, 0) == cudaSuccess;
+    for (size_t i = 0; ok && i < hs.size(); i++) ok = add_batch_branch(*hs[i], g, &body[i], &fixed);
+    g_kernel_launches.store(before);
+    if (ok && bg && bg->exec) {
+      cudaGraphExecUpdateResultInfo info;
+      if (cudaGraphExecUpdate(bg->exec, g, &info) != cudaSuccess) {
+        (void)cudaGetLastError();
+        cudaGraphExecDestroy(bg->exec);
+        bg->exec = nullptr;
+      }
+    }
+    if (ok && (!bg || !bg->exec)) {
+      if (!bg) bg = std::make_unique<BatchGraph>();
+      ok = cudaGraphInstantiate(&bg->exec, g, 0) == cudaSuccess;
+      if (!ok) bg->exec = nullptr;
+    }
+    if (g) cudaGraphDestroy(g);
+    if (!ok) {
+      (void)cudaGetLastError();
+      return false;
+    }
+    bg->hs = hs;
+    bg->gens = gens;
+    bg->body_kernels = body;
+    bg->fixed_kernels = fixed;
+  }
+  // the branches read what each handle's stream wrote (b, x, the hierarchy)
+  cudaEvent_t e0, e1;
+  FG_CUDA(cudaEventCreateWithFlags(&e0, cudaEventDefault));
+  FG_CUDA(cudaEventCreateWithFlags(&e1, cudaEventDefault));
+  for (Ctx* c : hs)
+    if (c->stream != s) {
+      cudaEvent_t w;
+      FG_CUDA(cudaEventCreateWithFlags(&w, cudaEventDisableTiming));
+      FG_CUDA(cudaEventRecord(w, c->stream));
+      FG_CUDA(cudaStreamWaitEvent(s, w, 0));
+      cudaEventDestroy(w);
+    }
+  FG_CUDA(cudaEventRecord(e0, s));
+  FG_CUDA(cudaGraphLaunch(bg->exec, s));
+  FG_CUDA(cudaEventRecord(e1, s));
+  FG_CUDA(cudaEventSynchronize(e1));
+  FG_CUDA(cudaEventElapsedTime(ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  res.assign(hs.size(), SolveResult());
+  int64_t kernels = bg->fixed_kernels;
+  for (size_t i = 0; i < hs.size(); i++) {
+    const double* h = hs[i]->h_scalars;
+    SolveResult& r = res[i];
+    r.iterations = (int)h[S_IT];
+    const double nr = sqrt(h[S_NR]), bnorm = h[S_BNORM];
+    r.relres = nr / bnorm;
+    kernels += bg->body_kernels[i] * r.iterations;
+    if (h[S_KERR] != 0.0) r.status = FEMGPU_ERR_LIMIT;
+    else if (h[S_FLAG] != 0.0 || !std::isfinite(nr)) r.status = FEMGPU_ERR_BREAKDOWN;
+    else if (r.relres <= hs[i]->cfg.tolerance) r.status = FEMGPU_OK;
+    else r.status = FEMGPU_ERR_NOT_CONVERGED;
+  }
+  g_kernel_launches.fetch_add(kernels);
+  g_batch.push_front(std::move(bg));
+  while (g_batch.size() > kBatchGraphsKept) g_batch.pop_back();
+  return true;
+}
+
+void batch_forget(Ctx* c) {
+  std::lock_guard<std::mutex> lock(g_batch_mu);
+  for (auto it = g_batch.begin(); it != g_batch.end();)
+    if (std::find((*it)->hs.begin(), (*it)->hs.end(), c) != (*it)->hs.end()) it = g_batch.erase(it);
+    else ++it;
 }
 
 namespace {

@@ -5,6 +5,7 @@
 // tetmesh.cu:257-260); the message is kept on the handle (femgpu_last_error).
 #include <algorithm>
 #include <atomic>
+#include <cstdlib>
 #include <cstring>
 #include <functional>
 #include <thread>
@@ -249,6 +250,7 @@ femgpu_status femgpu_destroy(femgpu_handle h) {
   cudaStream_t s = h->stream;
   bool own = h->own_stream;
   cudaMemPool_t pool = h->own_pool ? h->pool : nullptr;
+  batch_forget(h);  // kept batch graphs that point into this handle's buffers
   if (h->h_scalars) cudaFreeHost(h->h_scalars);
   delete h;  // buffers free asynchronously on s
   cudaStreamSynchronize(s);
@@ -535,26 +537,73 @@ femgpu_status femgpu_solve_batch(int count, femgpu_handle* hs, const double* con
   std::sort(streams.begin(), streams.end());
   if (std::adjacent_find(streams.begin(), streams.end()) != streams.end()) return FEMGPU_ERR_INVALID;
   std::vector<femgpu_status> status(count, FEMGPU_OK);
-  std::atomic<int> next{0};
-  auto work = [&]() {
-    for (int i = next.fetch_add(1); i < count; i = next.fetch_add(1)) {
-      femgpu_status st = setup ? femgpu_setup(hs[i]) : FEMGPU_OK;
-      if (st == FEMGPU_OK) st = femgpu_solve(hs[i], b[i], x[i], stats ? &stats[i] : nullptr);
-      status[i] = st;
+  // jobs spread over host threads (each handle's size reads and flags overlap the others')
+  auto run_threads = [&](const std::function<femgpu_status(int)>& job) {
+    std::atomic<int> next{0};
+    auto work = [&]() {
+      for (int i = next.fetch_add(1); i < count; i = next.fetch_add(1))
+        if (status[i] == FEMGPU_OK) status[i] = job(i);  // a handle whose setup failed is done
+    };
+    const int nt = threads == 0 ? count : std::min(threads, count);
+    std::vector<std::thread> pool;
+    try {
+      for (int t = 1; t < nt; t++) pool.emplace_back(work);
+    } catch (...) {
+      // fewer threads than asked (the remaining work is shared by the ones running)
     }
+    work();
+    for (auto& t : pool) t.join();
+    for (int i = 0; i < count; i++)
+      if (status[i] != FEMGPU_OK) return status[i];
+    return FEMGPU_OK;
   };
-  const int nt = threads == 0 ? count : std::min(threads, count);
-  std::vector<std::thread> pool;
-  try {
-    for (int t = 1; t < nt; t++) pool.emplace_back(work);
-  } catch (...) {
-    // fewer threads than asked (the remaining work is shared by the ones running)
+  bool graph = !getenv("FEMGPU_HOST_LOOP");
+  if (setup) graph = run_threads([&](int i) { return femgpu_setup(hs[i]); }) == FEMGPU_OK && graph;
+  // PCG solves of handles on one device: one graph launch with a branch per handle
+  for (int i = 0; graph && i < count; i++)
+    graph = hs[i]->cfg.solverType == 1 && hs[i]->cfg.maxIters > 0 && hs[i]->device == hs[0]->device &&
+            hs[i]->has_hierarchy;
+  if (graph) {
+    for (int i = 0; i < count; i++) {
+      femgpu_status st = guard(hs[i], [&] {
+        Ctx& c = *hs[i];
+        batch_prepare(c);
+        c.bat_b.upload(b[i], c.A.n);
+        c.bat_x.upload(x[i], c.A.n);
+      });
+      if (st != FEMGPU_OK) return st;
+    }
+    std::vector<Ctx*> list(hs, hs + count);
+    std::vector<SolveResult> res;
+    float ms = 0.0f;
+    bool ran = false;
+    femgpu_status st = guard(hs[0], [&] { ran = batch_solve_graph(list, res, &ms); });
+    if (st != FEMGPU_OK) return st;
+    if (ran) {
+      femgpu_status result = FEMGPU_OK;
+      for (int i = 0; i < count; i++) {
+        Ctx& c = *hs[i];
+        st = guard(hs[i], [&] {
+          c.bat_x.download(x[i], c.A.n);
+          FG_CUDA(cudaStreamSynchronize(c.stream));
+        });
+        if (st != FEMGPU_OK) return st;
+        if (stats) {
+          stats[i].iterations = res[i].iterations;
+          stats[i].relative_residual = res[i].relres;
+          stats[i].setup_ms = c.setup_ms;
+          stats[i].solve_ms = ms;  // the whole batch graph (the branches run together)
+          stats[i].num_levels = c.H ? c.H->num_levels : 0;
+        }
+        if (res[i].status == FEMGPU_ERR_NOT_CONVERGED) c.last_error = "PCG reached maxIters";
+        if (res[i].status == FEMGPU_ERR_BREAKDOWN) c.last_error = "PCG breakdown (non-positive curvature or NaN)";
+        if (res[i].status == FEMGPU_ERR_LIMIT) c.last_error = "smoother copy wait ran out";
+        if (res[i].status != FEMGPU_OK && result == FEMGPU_OK) result = res[i].status;
+      }
+      return result;
+    }
   }
-  work();
-  for (auto& t : pool) t.join();
-  for (int i = 0; i < count; i++)
-    if (status[i] != FEMGPU_OK) return status[i];
-  return FEMGPU_OK;
+  return run_threads([&](int i) { return femgpu_solve(hs[i], b[i], x[i], stats ? &stats[i] : nullptr); });
 }
 
 femgpu_status femgpu_adjoint_grad_device(femgpu_handle h, const double* d_dLdu, const double* d_u,

@@ -203,6 +203,8 @@ struct Ctx {
   double* noalloc_scratch = nullptr;
   // stage timing of a V-cycle run outside capture (FEMGPU_PROFILE set): named events
   std::vector<std::pair<std::string, cudaEvent_t>>* stage_marks = nullptr;
+  // b and x of this handle's branch in a batch graph (original numbering)
+  DBuf<double> bat_b, bat_x;
 
   ~Ctx() {
     if (pcg_exec) cudaGraphExecDestroy(pcg_exec);
@@ -250,6 +252,14 @@ void plan_smoother(Ctx& c, Level<T>& L);
 // keeps the fastest (cached per device and level shape); no-op when cfg.autotune is 0.
 template <class T>
 void autotune_level(Ctx& c, Level<T>& L);
+// The PCG solves of several handles (same device, hierarchies built) as one CUDA graph
+// launched on hs[0]'s stream: per handle an independent branch with its own device-side
+// loop, reading b and x from c.bat_b / c.bat_x (filled by the caller after batch_prepare)
+// and writing x back there.  The graph is kept per handle list and recaptured when a
+// hierarchy changes.  Returns false when the graph could not be built (nothing ran).
+void batch_prepare(Ctx& c);
+bool batch_solve_graph(const std::vector<Ctx*>& hs, std::vector<SolveResult>& res, float* ms);
+void batch_forget(Ctx* c);  // drops the kept graphs that use c (before c is destroyed)
 void amg_vcycle_device(Ctx& c, const double* d_r, double* d_z);
 void spmv_original(Ctx& c, const double* d_x, double* d_y);
 void profile_kernel(Ctx& c, int which, int reps, double* ms, double* bytes);

@@ -61,3 +61,34 @@ def test_batch_rejects_handles_on_one_stream():
     p2 = problem(4, 9, stream=stream.cuda_stream)
     xs, stats, status = femgpu.solve_batch([p1[0], p2[0]], [p1[1], p2[1]], check=False)
     assert status == 1  # FEMGPU_ERR_INVALID: their PCG captures would share the stream
+
+
+def test_batch_graph_is_kept_and_recaptured():
+    # second call: the kept graph (same handles, same hierarchies); third: new hierarchies
+    # (setup again) recaptured into the same graph; a zero right-hand side skips its loop
+    sizes = np.random.default_rng(3).integers(3, 9, size=5)
+    probs = [problem(int(n), 20 + i) for i, n in enumerate(sizes)]
+    solvers, bs = [p[0] for p in probs], [p[1] for p in probs]
+    bs[2] = np.zeros_like(bs[2])
+    first, _, status = femgpu.solve_batch(solvers, bs)
+    assert status == 0
+    for setup in (False, True):
+        xs, stats, status = femgpu.solve_batch(solvers, bs, setup=setup)
+        assert status == 0
+        for x, x0 in zip(xs, first):
+            assert np.array_equal(x, x0)
+    assert stats[2]["iterations"] == 0 and not xs[2].any()
+    for s, b, x in zip(solvers, bs, xs):
+        x1, st1 = s.solve(b)
+        assert np.array_equal(x, x1)
+
+
+def test_batch_host_threads_match_the_graph(monkeypatch):
+    sizes = np.random.default_rng(4).integers(3, 9, size=4)
+    probs = [problem(int(n), 30 + i) for i, n in enumerate(sizes)]
+    solvers, bs = [p[0] for p in probs], [p[1] for p in probs]
+    xg, sg, _ = femgpu.solve_batch(solvers, bs)
+    monkeypatch.setenv("FEMGPU_HOST_LOOP", "1")
+    xt, st, _ = femgpu.solve_batch(solvers, bs)
+    for a, b_, u, v in zip(xg, xt, sg, st):
+        assert np.array_equal(a, b_) and u["iterations"] == v["iterations"]
