@@ -1589,20 +1589,97 @@ __global__ void hash_block_kernel(EscArgs<T> a, const int32_t* rows, int nrows, 
   }
 }
 
+// Galerkin-product rows of a narrow product (at most kDenseCols output columns, few
+// rows): one warp per row with a dense accumulator over the output columns in shared
+// memory.  The left row's entries are taken in order, and for each of them the lanes take
+// the right row's entries, whose columns are distinct; so every column is summed in
+// generation order, its first product starting the sum -- the sums of the hash tiers,
+// without their probing.  Columns are listed as they are first hit, the list is sorted,
+// and the row is written in ascending column order into its temporary slots.
+constexpr int kDenseCols = 4096;
+template <class T>
+__host__ __device__ inline size_t dense_warp_smem(int ncols) {
+  const size_t acc = ((size_t)ncols * sizeof(T) + 15) / 16 * 16;
+  const size_t list = (size_t)next_pow2(ncols < 2 ? 2 : ncols) * sizeof(int32_t);
+  const size_t mark = ((size_t)ncols + 15) / 16 * 16;
+  return acc + list + mark;
+}
+
+template <class T>
+__global__ void spgemm_dense_warp_kernel(EscArgs<T> a, int ncols, const int32_t* __restrict__ toff,
+                                         int32_t* __restrict__ tci, T* __restrict__ tv, int32_t* __restrict__ counts) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const size_t per = dense_warp_smem<T>(ncols);
+  unsigned char* base = smem_raw + (size_t)w * per;
+  T* acc = reinterpret_cast<T*>(base);
+  int32_t* list = reinterpret_cast<int32_t*>(base + ((size_t)ncols * sizeof(T) + 15) / 16 * 16);
+  const int cap = next_pow2(ncols < 2 ? 2 : ncols);
+  unsigned char* mark = reinterpret_cast<unsigned char*>(list + cap);
+  for (int k = lane; k < ncols; k += 32) mark[k] = 0;
+  __syncwarp();
+  const unsigned below = (1u << lane) - 1u;
+  for (int i = blockIdx.x * nw + w; i < a.n; i += gridDim.x * nw) {
+    int nt = 0;
+    const int q1 = a.arp[i + 1];
+    for (int q = a.arp[i]; q < q1; q++) {
+      const int j = a.aci[q];
+      const T av = a.av[q];
+      const int b1 = a.brp[j + 1];
+      for (int f0 = a.brp[j]; f0 < b1; f0 += 32) {
+        const int f = f0 + lane;
+        const bool live = f < b1;
+        int col = 0;
+        T v = (T)0;
+        if (live) {
+          col = a.bci[f];
+          v = av * a.bv[f];
+        }
+        const bool fresh = live && mark[col] == 0;
+        if (fresh) {
+          mark[col] = 1;
+          acc[col] = v;
+        } else if (live) {
+          acc[col] = acc[col] + v;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, fresh);
+        if (fresh) list[nt + __popc(m & below)] = col;
+        nt += __popc(m);
+        __syncwarp();
+      }
+    }
+    const int np2 = next_pow2(nt < 2 ? 2 : nt);
+    for (int t = nt + lane; t < np2; t += 32) list[t] = INT32_MAX;
+    __syncwarp();
+    bitonic_sort_shared(list, np2, lane, 32, WarpSync());
+    const int o = toff[i];
+    for (int t = lane; t < nt; t += 32) {
+      const int col = list[t];
+      tci[o + t] = col;
+      tv[o + t] = acc[col];
+      mark[col] = 0;
+    }
+    if (lane == 0) counts[i] = nt;
+    __syncwarp();
+  }
+}
+
 __global__ void spgemm_capacity_kernel(int n, const int32_t* items, int ncols, int32_t* cap) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) cap[i] = min(items[i], ncols);
 }
 
-template <class T>
+// Rows from their capacity-spaced temporary slots to the compact CSR: G lanes per row
+// (G near the average row length, so short rows do not leave most of a warp idle).
+template <class T, int G>
 __global__ void compact_rows_copy_kernel(int n, const int32_t* toff, const int32_t* tci, const T* tv,
                                          const int32_t* orp, int32_t* oci, T* ov) {
-  const int lane = threadIdx.x & 31;
-  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += (gridDim.x * blockDim.x) >> 5) {
-    const int len = orp[i + 1] - orp[i];
-    for (int t = lane; t < len; t += 32) {
-      oci[orp[i] + t] = tci[toff[i] + t];
-      ov[orp[i] + t] = tv[toff[i] + t];
+  const int lane = threadIdx.x & (G - 1);
+  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) / G; i < n; i += (gridDim.x * blockDim.x) / G) {
+    const int o = orp[i], len = orp[i + 1] - o, src = toff[i];
+    for (int t = lane; t < len; t += G) {
+      oci[o + t] = tci[src + t];
+      ov[o + t] = tv[src + t];
     }
   }
 }
@@ -1625,7 +1702,15 @@ void run_spgemm_hash(Ctx& c, EscArgs<T> a, int nrows_out, int ncols_out, DCsr<T>
   nover1.zero();
   nover2.zero();
   const int wgrid = std::min<int64_t>((nrows_out + kHashWarps - 1) / kHashWarps, 152 * 32);
-  if (nrows_out >= 65536 && tcap <= (int64_t)nrows_out * 128) {
+  const size_t dper = dense_warp_smem<T>(ncols_out);
+  if (nrows_out < 65536 && ncols_out <= kDenseCols) {
+    // a narrow product: every row on the dense accumulator tier (no overflow rows)
+    const int wpb = (int)std::max<size_t>(1, std::min<size_t>(8, (size_t)(200 * 1024) / dper));
+    const size_t dsm = (size_t)wpb * dper;
+    if (dsm > 48 * 1024) ensure_smem(spgemm_dense_warp_kernel<T>, dsm);
+    FG_LAUNCH(spgemm_dense_warp_kernel<T>, (int)std::min<int64_t>((nrows_out + wpb - 1) / wpb, 152 * 4), 32 * wpb,
+              dsm, s, a, ncols_out, toff.p, tci.p, tv.p, cnt.p);
+  } else if (nrows_out >= 65536 && tcap <= (int64_t)nrows_out * 128) {
     // short rows on average: thread-per-row tier first, its overflow rows to the warp tier
     DBuf<int32_t> over0(nrows_out + 1, s), nover0(1, s);
     nover0.zero();
@@ -1682,8 +1767,21 @@ void run_spgemm_hash(Ctx& c, EscArgs<T> a, int nrows_out, int ncols_out, DCsr<T>
   pt.mark("sp big");
   out.ci.alloc(out.nnz > 0 ? out.nnz : 1, s);
   out.v.alloc(out.nnz > 0 ? out.nnz : 1, s);
-  FG_LAUNCH(compact_rows_copy_kernel<T>, grid_for((int64_t)nrows_out * 32, 256), 256, 0, s, nrows_out, toff.p, tci.p,
-            tv.p, out.rp.p, out.ci.p, out.v.p);
+  {
+    const double avg = nrows_out > 0 ? (double)out.nnz / nrows_out : 0.0;
+    const int G = avg <= 6.0 ? 4 : avg <= 12.0 ? 8 : avg <= 24.0 ? 16 : 32;
+    const int cgrid = grid_for((int64_t)nrows_out * G, 256);
+#define FG_COMPACT(GG)                                                                                    \
+  FG_LAUNCH((compact_rows_copy_kernel<T, GG>), cgrid, 256, 0, s, nrows_out, toff.p, tci.p, tv.p, out.rp.p, \
+            out.ci.p, out.v.p)
+    switch (G) {
+      case 4: FG_COMPACT(4); break;
+      case 8: FG_COMPACT(8); break;
+      case 16: FG_COMPACT(16); break;
+      default: FG_COMPACT(32); break;
+    }
+#undef FG_COMPACT
+  }
   pt.mark("sp out");
 }
 

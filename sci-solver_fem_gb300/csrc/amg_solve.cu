@@ -32,6 +32,11 @@ namespace cg = cooperative_groups;
 
 namespace femgpu {
 
+// Programmatic dependent launch of the solve kernels (on unless FEMGPU_NO_PDL is set, a
+// diagnostic switch for timing the same kernels with plain stream ordering).
+bool g_pdl_enabled = getenv("FEMGPU_NO_PDL") == nullptr;
+thread_local bool t_pdl_scope = false;
+
 namespace {
 
 constexpr int kRedBlocks = 608;  // 4 x 152 SMs: fixed grid for deterministic reductions
@@ -62,12 +67,14 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
 // ---- level kernels -----------------------------------------------------------------
 template <class T>
 __global__ void cast_in_kernel(int n, const double* in, T* out) {
+  pdl_enter();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = (T)in[i];
 }
 
 template <class T>
 __global__ void cast_out_kernel(int n, const T* in, double* out) {
+  pdl_enter();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = (double)in[i];
 }
@@ -155,6 +162,7 @@ __global__ void __launch_bounds__(1024) smooth_cluster_kernel(
     const int32_t* __restrict__ oci, const T* __restrict__ ov, const T* __restrict__ diag,
     const T* __restrict__ dinv, const T* __restrict__ b, T w, int inner, const T* __restrict__ x_in,
     T* __restrict__ x_out, T* __restrict__ r_out, int mcap, int scap, int ecap) {
+  pdl_enter();
   extern __shared__ __align__(128) unsigned char sm[];
   cg::cluster_group cl = cg::this_cluster();
   const int C = (int)cl.num_blocks();
@@ -243,10 +251,6 @@ __global__ void __launch_bounds__(1024) smooth_creg_kernel(
   const int rs = grows[g], m = grows[g + 1] - rs;
   const int qs = (m + C - 1) / C;
   const int ss = min(m, c * qs), ns = min(m, ss + qs) - ss;  // own slice: group rows [ss, ss + ns)
-  for (int t = threadIdx.x; t < m; t += blockDim.x) {
-    const int row = rs + t;
-    xa[t] = POST ? x_in[row] : (w * b[row]) * dinv[row];
-  }
   if (threadIdx.x == 0) {
     xa[mcap] = (T)0;
     xb[mcap] = (T)0;
@@ -254,6 +258,8 @@ __global__ void __launch_bounds__(1024) smooth_creg_kernel(
   const int t = threadIdx.x / S, j = threadIdx.x & (S - 1);
   const bool live = t < ns;
   const int row = rs + ss + t;
+  // the operator's entries, diagonal and row bounds are constant: loaded before waiting
+  // for the kernels that write b and x_in
   int e0 = 0, len = 0;
   T d = (T)1, di = (T)1, bb = (T)0, x = (T)0;
   if (live) {
@@ -261,8 +267,6 @@ __global__ void __launch_bounds__(1024) smooth_creg_kernel(
     len = irp[row + 1] - e0;
     d = diag[row];
     di = dinv[row];
-    bb = b[row];
-    x = POST ? x_in[row] : (w * bb) * di;
   }
   T val[K];
   uint32_t offp[K / 2];  // two 16-bit local columns per register
@@ -275,6 +279,15 @@ __global__ void __launch_bounds__(1024) smooth_creg_kernel(
     const uint32_t o0 = a0 ? (uint32_t)(ici[e0 + q0] - rs) : (uint32_t)mcap;
     const uint32_t o1 = a1 ? (uint32_t)(ici[e0 + q1] - rs) : (uint32_t)mcap;
     offp[k >> 1] = o0 | (o1 << 16);
+  }
+  pdl_enter();
+  for (int tt = threadIdx.x; tt < m; tt += blockDim.x) {
+    const int r = rs + tt;
+    xa[tt] = POST ? x_in[r] : (w * b[r]) * dinv[r];
+  }
+  if (live) {
+    bb = b[row];
+    x = POST ? x_in[row] : (w * bb) * di;
   }
   cl.sync();  // every CTA of the cluster is running and holds x0
   const T* cur = xa;
@@ -365,17 +378,22 @@ __host__ __device__ inline RegSmemLayout reg_smem_layout(int ecap) {
   return L;
 }
 
-// One thread (thread 0) starts the bulk copies of group g's values and columns into
-// staging buffer `buf`; completion is counted on bar[buf].  The group's entries are one
-// contiguous range in the jagged-diagonal arrays (the reordering stays inside each
-// 32-row block).
+// One thread (thread 0) starts the bulk copies of a group's values and columns (entries
+// [es, ee) of the jagged-diagonal arrays) into staging buffer `buf`; completion is counted
+// on bar[buf].  A group's entries are one contiguous range (the reordering stays inside
+// each 32-row block).  With orp (post relax), the group's cross-partition entries
+// [o0, o1), also one contiguous range, are prefetched into L2 for the b - A_out x that
+// opens the group.
 template <class T>
 __device__ __forceinline__ void stage_group(unsigned char* sm, const RegSmemLayout& Ls, uint64_t* bar, int buf,
-                                            int g, const int32_t* __restrict__ grows,
-                                            const int32_t* __restrict__ irp, const uint16_t* __restrict__ jc,
-                                            const T* __restrict__ jv) {
+                                            int es, int ee, const uint16_t* __restrict__ jc,
+                                            const T* __restrict__ jv, const int32_t* __restrict__ oci = nullptr,
+                                            const T* __restrict__ ov = nullptr, int o0 = 0, int o1 = 0) {
   constexpr int VA = 16 / (int)sizeof(T);
-  const int es = irp[grows[g]], ee = irp[grows[g + 1]];
+  if (oci) {
+    bulk_prefetch_range_l2(oci + o0, oci + o1);
+    bulk_prefetch_range_l2(ov + o0, ov + o1);
+  }
   const int v0 = es & ~(VA - 1), c0 = es & ~7;
   const uint32_t vbytes = (uint32_t)((((ee + VA - 1) & ~(VA - 1)) - v0) * (int)sizeof(T));
   const uint32_t cbytes = (uint32_t)((((ee + 7) & ~7) - c0) * 2);
@@ -428,20 +446,62 @@ __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
   constexpr int CS = xcopy_stride<T>();
   constexpr int VA = 16 / (int)sizeof(T);
   const int t = threadIdx.x, lane = t & 31;
+  // Group bounds travel across iterations, so no warp waits on a dependent global load
+  // at a group's start: rows [rs, re) of this group and [rsn, ren) of the next one; thread
+  // 0 also holds the next group's entry range [esn, een) and cross-partition range
+  // [osn, oen) for the staging it starts, and sh_es[buf] is the entry offset where the
+  // group staged into buffer buf begins.
+  __shared__ int sh_es[2];
+  const int g0 = blockIdx.x;
+  int rs = 0, re = 0, rsn = 0, ren = 0, esn = 0, een = 0, osn = 0, oen = 0;
+  if (g0 < ngroups) {
+    rs = grows[g0];
+    re = grows[g0 + 1];
+  }
+  if (g0 + (int)gridDim.x < ngroups) {
+    rsn = grows[g0 + gridDim.x];
+    ren = grows[g0 + gridDim.x + 1];
+  }
   if (t == 0) {
     mbar_init(bar, 1);
     mbar_init(bar + 1, 1);
+    // zero slot of both x buffers (slot kRegGroupRows of copy 0)
+    xa[kRegGroupRows] = (T)0;
+    xb[kRegGroupRows] = (T)0;
+    if (g0 < ngroups) {
+      const int es0 = irp[rs];
+      sh_es[0] = es0;
+      stage_group<T>(sm, Ls, bar, 0, es0, irp[re], jc, jv);
+    }
+    if (g0 + (int)gridDim.x < ngroups) {
+      esn = irp[rsn];
+      een = irp[ren];
+      if (orp) {
+        osn = orp[rsn];
+        oen = orp[ren];
+      }
+    }
   }
   __syncthreads();
-  if (t == 0 && (int)blockIdx.x < ngroups) stage_group<T>(sm, Ls, bar, 0, blockIdx.x, grows, irp, jc, jv);
+  // everything above reads constant data (group bounds, entry offsets) and writes only
+  // this CTA's shared memory
+  pdl_enter();
   int i = 0;
-  for (int g = blockIdx.x; g < ngroups; g += gridDim.x, i++) {
+  for (int g = g0; g < ngroups; g += gridDim.x, i++) {
     const int buf = i & 1;
     const uint32_t parity = (uint32_t)(i >> 1) & 1u;
-    const int gn = g + gridDim.x;
+    const int gn = g + gridDim.x, gn2 = gn + gridDim.x;
     // buffer buf ^ 1 was last read before the barrier that ended the previous group
-    if (t == 0 && gn < ngroups) stage_group<T>(sm, Ls, bar, buf ^ 1, gn, grows, irp, jc, jv);
-    const int rs = grows[g], re = grows[g + 1];
+    if (t == 0 && gn < ngroups) {
+      sh_es[buf ^ 1] = esn;
+      stage_group<T>(sm, Ls, bar, buf ^ 1, esn, een, jc, jv, orp ? oci : nullptr, ov, osn, oen);
+    }
+    // the bounds of the group after next, used from the next iteration on
+    int rsn2 = 0, ren2 = 0;
+    if (gn2 < ngroups) {
+      rsn2 = grows[gn2];
+      ren2 = grows[gn2 + 1];
+    }
     const int wb = rs + (t & ~31);  // first row of this warp's 32-row block
     const bool live = rs + t < re;
     // Every per-row input is loaded in the block's natural order (lane p loads row wb + p,
@@ -474,8 +534,8 @@ __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
     }
     // the next group's per-row inputs into L2 while this group is smoothed
     if (gn < ngroups) {
-      const int nr2 = grows[gn] + t;
-      if (nr2 < grows[gn + 1]) {
+      const int nr2 = rsn + t;
+      if (nr2 < ren) {
         prefetch_l2(jrow + nr2);
         prefetch_l2(irp + nr2);
         prefetch_l2(diag + nr2);
@@ -512,12 +572,16 @@ __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
     }
     const int kmax = __shfl_sync(0xffffffffu, len, 0);  // lane 0 holds the block's longest row
     const bool ok = mbar_wait_bounded(bar + buf, parity, wait_limit);
+    // Entry k of this lane's row: its value, and the byte offset of the x it reads within
+    // an x buffer (column + copy stride, times sizeof(T): below 2^16), two per register.
+    // Entries past the row's end hold value 0 and the offset of the zero slot.
     T val[K];
-    uint32_t offp[K / 2];  // two 16-bit columns per register
+    uint32_t offp[K / 2];
     {
-      const int es = irp[rs];
-      // the block's entries start where its first row's do (the reordering stays in the block)
-      const int eb = live ? irp[wb] : 0;
+      const int es = sh_es[buf];
+      // the block's entries start where its first row's do (the reordering stays in the
+      // block): lane 0 loaded that row's offset
+      const int eb = __shfl_sync(0xffffffffu, ne0, 0);
       const T* sval = reinterpret_cast<const T*>(sm + (buf ? Ls.val1 : Ls.val0)) + (eb - (es & ~(VA - 1)));
       const uint16_t* scol = reinterpret_cast<const uint16_t*>(sm + (buf ? Ls.col1 : Ls.col0)) + (eb - (es & ~7));
       int dk = lane;  // this lane's position on diagonal k
@@ -526,10 +590,20 @@ __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
         const unsigned m = __ballot_sync(0xffffffffu, k < len);
         const bool a = ok && k < len;
         val[k] = a ? sval[dk] : (T)0;
-        const uint32_t o = a ? (uint32_t)scol[dk] : 0u;
+        const uint32_t o = (a ? (uint32_t)scol[dk] : (uint32_t)kRegGroupRows) * (uint32_t)sizeof(T);
         if (k & 1) offp[k >> 1] |= o << 16;
         else offp[k >> 1] = o;
         dk += __popc(m);
+      }
+    }
+    // thread 0: the entry and cross-partition ranges of the group after next (its row
+    // bounds have arrived by now), for the staging it starts in the next iteration
+    if (t == 0 && gn2 < ngroups) {
+      esn = irp[rsn2];
+      een = irp[ren2];
+      if (orp) {
+        osn = orp[rsn2];
+        oen = orp[ren2];
       }
     }
     if (__syncthreads_or(!ok)) {
@@ -541,11 +615,23 @@ __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
       }
       return;
     }
+    // Fused multiply-adds in entry order, four entries per step while the block's longest
+    // row has entries left (a branch the whole warp takes alike).  An entry past the row's
+    // end adds 0 * 0 to the sum, which leaves it unchanged: the sum starts at +0 and an
+    // exact cancellation rounds to +0, so it is never -0.
     auto rowsum = [&](const T* src) {
+      const unsigned char* srcb = reinterpret_cast<const unsigned char*>(src);
       T sax = 0;
 #pragma unroll
-      for (int k = 0; k < K; k++)
-        if (k < kmax && k < len) sax = fma(val[k], src[(offp[k >> 1] >> ((k & 1) * 16)) & 0xffffu], sax);
+      for (int k0 = 0; k0 < K; k0 += 4) {
+        if (k0 < kmax) {
+#pragma unroll
+          for (int k = k0; k < k0 + 4; k++) {
+            const uint32_t o = (k & 1) ? offp[k >> 1] >> 16 : offp[k >> 1] & 0xffffu;
+            sax = fma(val[k], *reinterpret_cast<const T*>(srcb + o), sax);
+          }
+        }
+      }
       return sax;
     };
     auto sweep = [&](const T* src, T* dst) {
@@ -583,6 +669,10 @@ __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
       }
     }
     __syncthreads();  // x buffers and this staging buffer are free for the next group
+    rs = rsn;
+    re = ren;
+    rsn = rsn2;
+    ren = ren2;
   }
   if (POST && dot_part && z64) {
     const double t1 = block_sum(dz1, sh_dot);
@@ -607,6 +697,7 @@ __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
 template <class T>
 __global__ void aout_residual_kernel(int n, const int32_t* __restrict__ orp, const int32_t* __restrict__ oci,
                                      const T* __restrict__ ov, const T* __restrict__ x, T* __restrict__ r) {
+  pdl_enter();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const T ri = r[i];
@@ -620,11 +711,36 @@ __global__ void aout_residual_kernel(int n, const int32_t* __restrict__ orp, con
 template <class T, int S>
 __global__ void spmv_lanes_kernel(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
                                   const T* __restrict__ v, const T* __restrict__ x, T* __restrict__ y, int accumulate) {
+  constexpr int K = S == 1 ? 8 : 4;
   const int g = (blockIdx.x * blockDim.x + threadIdx.x) / S;
   const int j = threadIdx.x & (S - 1);
   const bool live = g < n;
+  // the operator's row bounds and first K entries of this lane are constant: loaded
+  // before waiting for the kernel that writes x
+  int e = 0, end = 0, c[K];
+  T a[K];
+  if (live) {
+    e = rp[g] + j;
+    end = rp[g + 1];
+  }
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    const int q = e + k * S;
+    c[k] = q < end ? ci[q] : 0;
+    a[k] = q < end ? v[q] : (T)0;
+  }
+  pdl_enter();
+  // the sum of gather_row: products rounded separately, added in entry order from 0
   T s = 0;
-  if (live) s = gather_row<T, (S == 1 ? 8 : 4), false>(ci, v, x, rp[g] + j, rp[g + 1], S, (T)0);
+  if (live) {
+    T xv[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) xv[k] = e + k * S < end ? x[c[k]] : (T)0;
+#pragma unroll
+    for (int k = 0; k < K; k++)
+      if (e + k * S < end) s = s + a[k] * xv[k];
+    for (int q = e + K * S; q < end; q += S) s = s + v[q] * x[ci[q]];
+  }
 #pragma unroll
   for (int off = S >> 1; off > 0; off >>= 1) s = s + __shfl_xor_sync(0xffffffffu, s, off, S);
   if (live && j == 0) y[g] = accumulate ? y[g] + s : s;
@@ -636,9 +752,21 @@ __global__ void spmv_lanes_kernel(int n, const int32_t* __restrict__ rp, const i
 template <class T>
 __global__ void coarse_solve_kernel(int n, const double* __restrict__ inv, const T* __restrict__ b, T* __restrict__ x) {
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  // the inverse is constant: this lane's first four entries are loaded before the wait
+  double iv[4];
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    const int j = lane + 32 * q;
+    iv[q] = i < n && j < n ? inv[(int64_t)i * n + j] : 0.0;
+  }
+  pdl_enter();
   double s = 0.0;
-  if (i < n)
-    for (int j = lane; j < n; j += 32) s = fma(inv[(int64_t)i * n + j], (double)b[j], s);
+  if (i < n) {
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+      if (lane + 32 * q < n) s = fma(iv[q], (double)b[lane + 32 * q], s);
+    for (int j = lane + 128; j < n; j += 32) s = fma(inv[(int64_t)i * n + j], (double)b[j], s);
+  }
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) s = s + __shfl_xor_sync(0xffffffffu, s, off);
   if (i < n && lane == 0) x[i] = (T)s;
@@ -749,6 +877,7 @@ __global__ void residual_kernel(int n, const double* __restrict__ b, const doubl
 __global__ void update_kernel(int n, double* __restrict__ sc, const double* __restrict__ p,
                               const double* __restrict__ y, double* __restrict__ x, double* __restrict__ r,
                               double* __restrict__ rold, double* partial, unsigned* counter) {
+  pdl_enter();
   __shared__ double sh[32];
   const double alpha = sc[S_ALPHA];
   double acc = 0.0;
@@ -817,6 +946,7 @@ __global__ void spmv_dot_kernel(int n, const int32_t* __restrict__ rp, const int
                                       const double* __restrict__ v, const double* __restrict__ p,
                                       double* __restrict__ y, double* __restrict__ partial, double* sc,
                                       unsigned* counter) {
+  pdl_enter();
   __shared__ double sh[32];
   double acc = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -885,6 +1015,7 @@ __global__ void spmv_dot_sliced_kernel(int n, const int32_t* __restrict__ off, c
                                        const double* __restrict__ v, const double* __restrict__ p,
                                        double* __restrict__ y, double* __restrict__ partial, double* sc,
                                        unsigned* counter) {
+  pdl_enter();
   __shared__ double sh[32];
   double acc = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -914,6 +1045,7 @@ __global__ void spmv_sliced_kernel(int n, const int32_t* __restrict__ off, const
 __global__ void dot_beta_kernel(int n, const double* __restrict__ z, const double* __restrict__ r,
                                 const double* __restrict__ rold, double* partial, double* partial2, double* sc,
                                 int flexible, unsigned* counter) {
+  pdl_enter();
   __shared__ double sh[32];
   double s1 = 0.0, s2 = 0.0;
   // elements i, i + G, ... in order; four at a time with all loads issued first
@@ -958,6 +1090,7 @@ __global__ void dot_beta_kernel(int n, const double* __restrict__ z, const doubl
 // sqrt(r.r) / |b| <= tol), breakdown, a non-finite residual, a smoother copy that
 // timed out, or maxIters.
 __global__ void pcg_check_kernel(double* sc, cudaGraphConditionalHandle loop) {
+  pdl_enter();
   const double it = sc[S_IT] + 1.0;
   sc[S_IT] = it;
   const double nr = sqrt(sc[S_NR]);
@@ -970,6 +1103,7 @@ __global__ void set_slot_kernel(double* sc, int slot, double v) { sc[slot] = v; 
 
 __global__ void pupdate_kernel(int n, const double* __restrict__ sc, const double* __restrict__ z,
                                double* __restrict__ p) {
+  pdl_enter();
   const double beta = sc[S_BETA];
   const int G = gridDim.x * blockDim.x;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1015,12 +1149,12 @@ void spmv_lanes(const DCsr<T>& M, const T* x, T* y, int accumulate, cudaStream_t
   const int64_t threads = (int64_t)M.n * S;
   const int g = grid_for(threads, 256);
   switch (S) {
-    case 1: FG_LAUNCH((spmv_lanes_kernel<T, 1>), g, 256, 0, st, M.n, M.rp.p, M.ci.p, M.v.p, x, y, accumulate); break;
-    case 2: FG_LAUNCH((spmv_lanes_kernel<T, 2>), g, 256, 0, st, M.n, M.rp.p, M.ci.p, M.v.p, x, y, accumulate); break;
-    case 4: FG_LAUNCH((spmv_lanes_kernel<T, 4>), g, 256, 0, st, M.n, M.rp.p, M.ci.p, M.v.p, x, y, accumulate); break;
-    case 8: FG_LAUNCH((spmv_lanes_kernel<T, 8>), g, 256, 0, st, M.n, M.rp.p, M.ci.p, M.v.p, x, y, accumulate); break;
-    case 16: FG_LAUNCH((spmv_lanes_kernel<T, 16>), g, 256, 0, st, M.n, M.rp.p, M.ci.p, M.v.p, x, y, accumulate); break;
-    default: FG_LAUNCH((spmv_lanes_kernel<T, 32>), g, 256, 0, st, M.n, M.rp.p, M.ci.p, M.v.p, x, y, accumulate); break;
+    case 1: FG_LAUNCH_PDL((spmv_lanes_kernel<T, 1>), g, 256, 0, st, M.n, M.rp.p, M.ci.p, M.v.p, x, y, accumulate); break;
+    case 2: FG_LAUNCH_PDL((spmv_lanes_kernel<T, 2>), g, 256, 0, st, M.n, M.rp.p, M.ci.p, M.v.p, x, y, accumulate); break;
+    case 4: FG_LAUNCH_PDL((spmv_lanes_kernel<T, 4>), g, 256, 0, st, M.n, M.rp.p, M.ci.p, M.v.p, x, y, accumulate); break;
+    case 8: FG_LAUNCH_PDL((spmv_lanes_kernel<T, 8>), g, 256, 0, st, M.n, M.rp.p, M.ci.p, M.v.p, x, y, accumulate); break;
+    case 16: FG_LAUNCH_PDL((spmv_lanes_kernel<T, 16>), g, 256, 0, st, M.n, M.rp.p, M.ci.p, M.v.p, x, y, accumulate); break;
+    default: FG_LAUNCH_PDL((spmv_lanes_kernel<T, 32>), g, 256, 0, st, M.n, M.rp.p, M.ci.p, M.v.p, x, y, accumulate); break;
   }
 }
 
@@ -1076,13 +1210,16 @@ void launch_clustered(void (*k)(KArgs...), int grid, int block, size_t smem, int
   cfg.blockDim = dim3((unsigned)block);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
-  cudaLaunchAttribute at[1];
+  cudaLaunchAttribute at[2];
   at[0].id = cudaLaunchAttributeClusterDimension;
   at[0].val.clusterDim.x = (unsigned)cluster;
   at[0].val.clusterDim.y = 1;
   at[0].val.clusterDim.z = 1;
+  // both clustered smoothers call pdl_wait() before they touch memory other kernels write
+  at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[1].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = at;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = g_pdl_enabled && t_pdl_scope ? 2 : 1;
   g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
   FG_CUDA(cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...));
 }
@@ -1107,6 +1244,7 @@ __global__ void slice_entries_kernel(int ngroups, int C, const int32_t* grows, c
 template <class T, bool RHS, int S>
 __global__ void aout_lanes_kernel(int n, const int32_t* __restrict__ orp, const int32_t* __restrict__ oci,
                                   const T* __restrict__ ov, const T* base, const T* __restrict__ x, T* out) {
+  pdl_enter();
   const int g = (blockIdx.x * blockDim.x + threadIdx.x) / S, j = threadIdx.x & (S - 1);
   const bool live = g < n;
   int a = 0, b = 0;
@@ -1161,7 +1299,7 @@ template <class T, bool RHS>
 void launch_aout_lanes(cudaStream_t st, const Level<T>& L, int S, const T* base, const T* x, T* out) {
   const int g = grid_for((int64_t)L.n * S, 256);
 #define FG_AOUT(SS)                                                                                   \
-  FG_LAUNCH((aout_lanes_kernel<T, RHS, SS>), g, 256, 0, st, L.n, L.Aout.rp.p, L.Aout.ci.p, L.Aout.v.p, base, x, out)
+  FG_LAUNCH_PDL((aout_lanes_kernel<T, RHS, SS>), g, 256, 0, st, L.n, L.Aout.rp.p, L.Aout.ci.p, L.Aout.v.p, base, x, out)
   switch (S) {
     case 2: FG_AOUT(2); break;
     case 4: FG_AOUT(4); break;
@@ -1181,6 +1319,7 @@ template <class T>
 __global__ void aout_rhs_kernel(int n, const int32_t* __restrict__ orp, const int32_t* __restrict__ oci,
                                 const T* __restrict__ ov, const T* __restrict__ b, const T* __restrict__ x,
                                 T* __restrict__ bp) {
+  pdl_enter();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   // acc + (-v) x and acc - v x round identically: the negation is exact
@@ -1193,7 +1332,7 @@ void aout_rhs(cudaStream_t s, const Level<T>& L, const T* b, const T* x, T* bp) 
   if (S > 1)
     launch_aout_lanes<T, true>(s, L, S, b, x, bp);
   else
-    FG_LAUNCH(aout_rhs_kernel<T>, grid_for(L.n, 256), 256, 0, s, L.n, L.Aout.rp.p, L.Aout.ci.p, L.Aout.v.p, b, x,
+    FG_LAUNCH_PDL(aout_rhs_kernel<T>, grid_for(L.n, 256), 256, 0, s, L.n, L.Aout.rp.p, L.Aout.ci.p, L.Aout.v.p, b, x,
               bp);
 }
 
@@ -1204,7 +1343,7 @@ void aout_residual(cudaStream_t s, const Level<T>& L, const T* x, T* r) {
   if (S > 1)
     launch_aout_lanes<T, false>(s, L, S, r, x, r);
   else
-    FG_LAUNCH(aout_residual_kernel<T>, grid_for(L.n, 256), 256, 0, s, L.n, L.Aout.rp.p, L.Aout.ci.p, L.Aout.v.p, x,
+    FG_LAUNCH_PDL(aout_residual_kernel<T>, grid_for(L.n, 256), 256, 0, s, L.n, L.Aout.rp.p, L.Aout.ci.p, L.Aout.v.p, x,
               r);
 }
 
@@ -1233,7 +1372,7 @@ void smooth_sweeps(Ctx& c, Level<T>& L, bool post, const T* b, const T* xin, T* 
     auto k = post ? smooth_reg_kernel<T, true, kRegRow> : smooth_reg_kernel<T, false, kRegRow>;
     if (L.smooth_smem > 48 * 1024)
       ensure_smem(k, L.smooth_smem);
-    FG_LAUNCH(k, L.smooth_grid, L.smooth_threads, L.smooth_smem, s, L.ngroups, L.grows.p, L.Ain.rp.p, L.jc16.p,
+    FG_LAUNCH_PDL(k, L.smooth_grid, L.smooth_threads, L.smooth_smem, s, L.ngroups, L.grows.p, L.Ain.rp.p, L.jc16.p,
               L.jv.p, L.jrow.p, L.diag.p, L.dinv.p, b, w, inner, xin, xout, rout, L.max_group_ents + 16,
               c.red.p + 2 * kRedBlocks + S_KERR, f.b64, f.b_store, f.aout ? L.Aout.rp.p : nullptr,
               f.aout ? L.Aout.ci.p : nullptr, f.aout ? L.Aout.v.p : nullptr, f.z64, f.dot_r, f.dot_o, f.dot_part,
@@ -1285,7 +1424,7 @@ void smooth(Ctx& c, Level<T>& L, bool post, const T* b, const T* xin, T* xout, T
     return;
   }
   if (!post && b64) {
-    FG_LAUNCH(cast_in_kernel<T>, grid_for(L.n, 256), 256, 0, s, L.n, b64, b_store);
+    FG_LAUNCH_PDL(cast_in_kernel<T>, grid_for(L.n, 256), 256, 0, s, L.n, b64, b_store);
     b = b_store;
   }
   if (post) {
@@ -1293,7 +1432,7 @@ void smooth(Ctx& c, Level<T>& L, bool post, const T* b, const T* xin, T* xout, T
     b = L.bp.p;
   }
   smooth_sweeps<T>(c, L, post, b, xin, xout, rout);
-  if (z64) FG_LAUNCH(cast_out_kernel<T>, grid_for(L.n, 256), 256, 0, s, L.n, xout, z64);
+  if (z64) FG_LAUNCH_PDL(cast_out_kernel<T>, grid_for(L.n, 256), 256, 0, s, L.n, xout, z64);
 }
 
 // Records a named event on the stream when stage timing is on (never during capture).
@@ -1310,12 +1449,14 @@ template <class T>
 __global__ void residual_rows_kernel(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
                                      const T* __restrict__ v, const T* __restrict__ b, const T* __restrict__ x,
                                      T* __restrict__ r) {
+  pdl_enter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) r[i] = gather_row<T, 8, true>(ci, v, x, rp[i], rp[i + 1], 1, b[i]);
 }
 
 template <class T>
 __global__ void add_into_kernel(int n, const T* __restrict__ d, T* __restrict__ x) {
+  pdl_enter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) x[i] = x[i] + d[i];
 }
@@ -1362,6 +1503,7 @@ template <class T>
 __global__ void l1_sweep_kernel(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
                                 const T* __restrict__ v, const T* __restrict__ b, const T* __restrict__ l1inv, T w,
                                 const T* __restrict__ xin, T* __restrict__ xout) {
+  pdl_enter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const T s = row_fma_sum(rp, ci, v, xin, i);
@@ -1373,6 +1515,7 @@ __global__ void l1_sweep_kernel(int n, const int32_t* __restrict__ rp, const int
 template <class T>
 __global__ void l1_first_sweep_kernel(int n, const T* __restrict__ b, const T* __restrict__ l1inv, T w,
                                       T* __restrict__ x) {
+  pdl_enter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) x[i] = (T)0 + (w * (b[i] - (T)0)) * l1inv[i];
 }
@@ -1382,6 +1525,7 @@ template <class T>
 __global__ void full_residual_kernel(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
                                      const T* __restrict__ v, const T* __restrict__ b, const T* __restrict__ x,
                                      T* __restrict__ r) {
+  pdl_enter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) r[i] = b[i] - row_fma_sum(rp, ci, v, x, i);
 }
@@ -1391,7 +1535,7 @@ template <class T>
 void l1_sweeps(Ctx& c, Level<T>& L, const T* b, int sweeps) {
   const T w = (T)c.cfg.smootherWeight;
   for (int it = 0; it < sweeps; it++) {
-    FG_LAUNCH(l1_sweep_kernel<T>, grid_for(L.n, 256), 256, 0, c.stream, L.n, L.Ap.rp.p, L.Ap.ci.p, L.Ap.v.p, b,
+    FG_LAUNCH_PDL(l1_sweep_kernel<T>, grid_for(L.n, 256), 256, 0, c.stream, L.n, L.Ap.rp.p, L.Ap.ci.p, L.Ap.v.p, b,
               L.l1inv.p, w, L.x.p, L.r.p);
     std::swap(L.x.p, L.r.p);
   }
@@ -1417,8 +1561,9 @@ void vcycle(Ctx& c, Hierarchy<T>& H, int l, T* b_in, T* x_out, double* z_out = n
   cudaStream_t s = c.stream;
   Level<T>& L = *H.L[l];
   const int n = L.A.n;
+  const PdlScope pdl_scope(n <= kPdlLevelRows);
   if (L.coarsest) {
-    FG_LAUNCH(coarse_solve_kernel<T>, grid_for((int64_t)n * 32, 256), 256, 0, s, n, L.Ainv.p, b_in, x_out);
+    FG_LAUNCH_PDL(coarse_solve_kernel<T>, grid_for((int64_t)n * 32, 256), 256, 0, s, n, L.Ainv.p, b_in, x_out);
     stage_mark(c, "coarse", l);
     return;
   }
@@ -1426,15 +1571,15 @@ void vcycle(Ctx& c, Hierarchy<T>& H, int l, T* b_in, T* x_out, double* z_out = n
   const bool l1 = c.cfg.smoother == 1;
   if (l1) {
     // l1-Jacobi from x = 0, then r = b - A x
-    if (r64) FG_LAUNCH(cast_in_kernel<T>, grid_for(n, 256), 256, 0, s, n, r64, b_in);
+    if (r64) FG_LAUNCH_PDL(cast_in_kernel<T>, grid_for(n, 256), 256, 0, s, n, r64, b_in);
     if (c.cfg.preInnerIters > 0) {
-      FG_LAUNCH(l1_first_sweep_kernel<T>, grid_for(n, 256), 256, 0, s, n, b, L.l1inv.p, (T)c.cfg.smootherWeight,
+      FG_LAUNCH_PDL(l1_first_sweep_kernel<T>, grid_for(n, 256), 256, 0, s, n, b, L.l1inv.p, (T)c.cfg.smootherWeight,
                 L.x.p);
       l1_sweeps(c, L, b, c.cfg.preInnerIters - 1);
     } else {
       FG_CUDA(cudaMemsetAsync(L.x.p, 0, (size_t)n * sizeof(T), s));
     }
-    FG_LAUNCH(full_residual_kernel<T>, grid_for(n, 256), 256, 0, s, n, L.Ap.rp.p, L.Ap.ci.p, L.Ap.v.p, b, L.x.p,
+    FG_LAUNCH_PDL(full_residual_kernel<T>, grid_for(n, 256), 256, 0, s, n, L.Ap.rp.p, L.Ap.ci.p, L.Ap.v.p, b, L.x.p,
               L.r.p);
     stage_mark(c, "pre", l);
   } else {
@@ -1452,10 +1597,10 @@ void vcycle(Ctx& c, Hierarchy<T>& H, int l, T* b_in, T* x_out, double* z_out = n
   vcycle(c, H, l + 1, bc, xc, nullptr, nullptr, cycle_first_visit(type));
   if (type != 0 && !N.coarsest) {
     FG_REQUIRE(N.wr.n == (size_t)N.n && N.wd.n == (size_t)N.n, FEMGPU_ERR_INVALID, "cycle work vectors missing");
-    FG_LAUNCH(residual_rows_kernel<T>, grid_for(N.n, 256), 256, 0, s, N.n, N.Ap.rp.p, N.Ap.ci.p, N.Ap.v.p, bc, xc,
+    FG_LAUNCH_PDL(residual_rows_kernel<T>, grid_for(N.n, 256), 256, 0, s, N.n, N.Ap.rp.p, N.Ap.ci.p, N.Ap.v.p, bc, xc,
               N.wr.p);
     vcycle(c, H, l + 1, N.wr.p, N.wd.p, nullptr, nullptr, cycle_second_visit(type));
-    FG_LAUNCH(add_into_kernel<T>, grid_for(N.n, 256), 256, 0, s, N.n, N.wd.p, xc);
+    FG_LAUNCH_PDL(add_into_kernel<T>, grid_for(N.n, 256), 256, 0, s, N.n, N.wd.p, xc);
   }
   spmv_lanes(L.P, xc, L.x.p, 1, s);
   stage_mark(c, "prolong", l);
@@ -1478,7 +1623,7 @@ void vcycle(Ctx& c, Hierarchy<T>& H, int l, T* b_in, T* x_out, double* z_out = n
   if (l > 0) {
     if (!out_done) FG_CUDA(cudaMemcpyAsync(x_out, L.x.p, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
   } else if (z_out) {
-    if (!z_done) FG_LAUNCH(cast_out_kernel<T>, grid_for(n, 256), 256, 0, s, n, L.x.p, z_out);
+    if (!z_done) FG_LAUNCH_PDL(cast_out_kernel<T>, grid_for(n, 256), 256, 0, s, n, L.x.p, z_out);
   } else {
     FG_CUDA(cudaMemcpyAsync(x_out, L.x.p, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
   }
@@ -1494,9 +1639,9 @@ void precondition(Ctx& c, Hierarchy<T>& H, const double* r, double* z) {
   T* b = L.coarsest ? L.b.p : L.t.p;
   T* x = L.coarsest ? L.x.p : L.xo.p;
   if (L.coarsest) {
-    FG_LAUNCH(cast_in_kernel<T>, grid_for(n, 256), 256, 0, s, n, r, b);
+    FG_LAUNCH_PDL(cast_in_kernel<T>, grid_for(n, 256), 256, 0, s, n, r, b);
     vcycle(c, H, 0, b, x);
-    FG_LAUNCH(cast_out_kernel<T>, grid_for(n, 256), 256, 0, s, n, x, z);
+    FG_LAUNCH_PDL(cast_out_kernel<T>, grid_for(n, 256), 256, 0, s, n, x, z);
   } else {
     vcycle(c, H, 0, b, x, z, r, c.cfg.cycleType);  // level 0 reads r and writes z itself
   }
@@ -1876,10 +2021,10 @@ namespace {
 void launch_spmv_dot(Ctx& c, int n, const double* p, double* y) {
   const DCsr<double>& A = c.A0p;
   if (c.sliced)
-    FG_LAUNCH(spmv_dot_sliced_kernel, kRedBlocks, kRedThreads, 0, c.stream, n, c.s_off.p, c.s_ci.p, c.s_v.p, p, y,
+    FG_LAUNCH_PDL(spmv_dot_sliced_kernel, kRedBlocks, kRedThreads, 0, c.stream, n, c.s_off.p, c.s_ci.p, c.s_v.p, p, y,
               c.red.p, c.red.p + 2 * kRedBlocks, c.rcount.p + 1);
   else
-    FG_LAUNCH(spmv_dot_kernel, kRedBlocks, kRedThreads, 0, c.stream, n, A.rp.p, A.ci.p, A.v.p, p, y, c.red.p,
+    FG_LAUNCH_PDL(spmv_dot_kernel, kRedBlocks, kRedThreads, 0, c.stream, n, A.rp.p, A.ci.p, A.v.p, p, y, c.red.p,
               c.red.p + 2 * kRedBlocks, c.rcount.p + 1);
 }
 
@@ -1911,11 +2056,11 @@ void pcg_iteration_body(Ctx& c, int n, int flexible, bool to_host) {
   }
   c.zdot = nullptr;
   if (!zd.done)  // else z.r (z.r_old) and beta came from the smoother that wrote z
-    FG_LAUNCH(dot_beta_kernel, kRedBlocks, kRedThreads, 0, s, n, c.vz.p, c.vr.p, flexible ? c.vrold.p : nullptr,
+    FG_LAUNCH_PDL(dot_beta_kernel, kRedBlocks, kRedThreads, 0, s, n, c.vz.p, c.vr.p, flexible ? c.vrold.p : nullptr,
               part, part2, sc, flexible, cnt);
-  FG_LAUNCH(pupdate_kernel, kRedBlocks, kRedThreads, 0, s, n, sc, c.vz.p, c.vp.p);
+  FG_LAUNCH_PDL(pupdate_kernel, kRedBlocks, kRedThreads, 0, s, n, sc, c.vz.p, c.vp.p);
   launch_spmv_dot(c, n, c.vp.p, c.vy.p);
-  FG_LAUNCH(update_kernel, kRedBlocks, kRedThreads, 0, s, n, sc, c.vp.p, c.vy.p, c.vx.p, c.vr.p,
+  FG_LAUNCH_PDL(update_kernel, kRedBlocks, kRedThreads, 0, s, n, sc, c.vp.p, c.vy.p, c.vx.p, c.vr.p,
             flexible ? c.vrold.p : nullptr, part, cnt + 2);
   if (to_host) FG_CUDA(cudaMemcpyAsync(c.h_scalars, sc, S_COUNT * sizeof(double), cudaMemcpyDeviceToHost, s));
 }
@@ -1941,7 +2086,7 @@ cudaGraphNode_t add_pcg_loop(Ctx& c, int n, int flexible, cudaGraph_t g, cudaGra
     return nullptr;
   try {
     pcg_iteration_body(c, n, flexible, false);
-    FG_LAUNCH(pcg_check_kernel, 1, 1, 0, s, c.red.p + 2 * kRedBlocks, loop);
+    FG_LAUNCH_PDL(pcg_check_kernel, 1, 1, 0, s, c.red.p + 2 * kRedBlocks, loop);
   } catch (...) {
     cudaGraph_t dummy = nullptr;
     cudaStreamEndCapture(s, &dummy);
@@ -1960,22 +2105,27 @@ bool capture_iteration(Ctx& c, int n, int flexible) {
   }
   int64_t before = g_kernel_launches.load();
   cudaGraph_t g = nullptr;
-  auto fail = [&]() {
-    (void)cudaGetLastError();
+  // a failed capture leaves the solve on the host-driven loop (same kernels); with
+  // FEMGPU_PROFILE the reason is printed
+  auto fail = [&](const char* where) {
+    const cudaError_t err = cudaGetLastError();
+    if (getenv("FEMGPU_PROFILE"))
+      fprintf(stderr, "[femgpu] PCG graph not used (%s: %s)\n", where, cudaGetErrorString(err));
     if (g) cudaGraphDestroy(g);
     g_kernel_launches.store(before);
     return false;
   };
-  if (cudaGraphCreate(&g, 0) != cudaSuccess) return fail();
+  if (cudaGraphCreate(&g, 0) != cudaSuccess) return fail("create");
   cudaGraphConditionalHandle loop;
-  if (cudaGraphConditionalHandleCreate(&loop, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) return fail();
-  if (!add_pcg_loop(c, n, flexible, g, loop, nullptr, 0)) return fail();
+  if (cudaGraphConditionalHandleCreate(&loop, g, 1, cudaGraphCondAssignDefault) != cudaSuccess)
+    return fail("conditional handle");
+  if (!add_pcg_loop(c, n, flexible, g, loop, nullptr, 0)) return fail("capture");
   cudaError_t e = cudaGraphInstantiate(&c.pcg_exec, g, 0);
   cudaGraphDestroy(g);
   g = nullptr;
   if (e != cudaSuccess) {
     c.pcg_exec = nullptr;
-    return fail();
+    return fail("instantiate");
   }
   c.graph_nodes = g_kernel_launches.load() - before;  // kernels of one iteration
   g_kernel_launches.store(before);  // counted per iteration after each solve
@@ -2313,7 +2463,7 @@ void profile_level0(Ctx& c, Hierarchy<T>& H, int which, int reps, double* ms, do
         }
         c.zdot = nullptr;
         if (!zd.done)
-          FG_LAUNCH(dot_beta_kernel, kRedBlocks, kRedThreads, 0, s, n, c.vz.p, c.vr.p, c.vrold.p, c.red.p,
+          FG_LAUNCH_PDL(dot_beta_kernel, kRedBlocks, kRedThreads, 0, s, n, c.vz.p, c.vr.p, c.vrold.p, c.red.p,
                     c.red.p + kRedBlocks, c.red.p + 2 * kRedBlocks, 1, c.rcount.p);
         break;
       }

@@ -207,9 +207,35 @@ __host__ __device__ inline int next_pow2(int v) {
   return p;
 }
 
+// Programmatic dependent launch.  A kernel launched with the programmatic
+// stream-serialisation attribute (launch_pdl) may be scheduled before the kernel ahead
+// of it in the stream has finished, once every CTA of that kernel has called
+// pdl_trigger() (or exited).  It must call pdl_wait() before it reads anything an
+// earlier kernel wrote and before it writes anything: pdl_wait() returns when the kernel
+// ahead has completed and its memory operations are visible.  What it reads before
+// pdl_wait() must be constant across the kernels of the stream (matrix entries, sizes).
+// In a kernel launched without the attribute both are no-ops.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+// The start of a kernel that reads nothing before waiting: wait, then let the next
+// kernel be scheduled.
+__device__ __forceinline__ void pdl_enter() {
+  pdl_wait();
+  pdl_trigger();
+}
+
 // A hint to bring the line holding p into L2 (p must point into an allocation).
 __device__ __forceinline__ void prefetch_l2(const void* p) {
   asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
+// A bulk asynchronous prefetch of the 16-byte units that lie wholly inside [b, e) into
+// L2 (both ends rounded down to 16 bytes, so nothing past e is touched; b must point
+// into an allocation, whose start is 16-byte aligned).  Nothing waits for it.
+__device__ __forceinline__ void bulk_prefetch_range_l2(const void* b, const void* e) {
+  const uintptr_t lo = (uintptr_t)b & ~(uintptr_t)15, hi = (uintptr_t)e & ~(uintptr_t)15;
+  if (hi > lo)
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(lo), "r"((uint32_t)(hi - lo)) : "memory");
 }
 
 // ---- bulk asynchronous copies (TMA, 1-D) with an mbarrier -----------------------

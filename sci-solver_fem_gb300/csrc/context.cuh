@@ -29,6 +29,42 @@ extern std::atomic<int64_t> g_kernel_launches;
     FG_CHECK_LAUNCH();                                                        \
   } while (0)
 
+// A kernel launch with programmatic dependent launch (the kernel calls pdl_wait() before
+// it touches memory that other kernels write), counted like FG_LAUNCH.  The attribute is
+// set only inside a PdlScope that allows it: the V-cycle of a level with at most
+// kPdlLevelRows rows, whose small kernels are bound by launch latency.  Elsewhere (the
+// large level-0 kernels, the PCG vector kernels) early-scheduled successors waiting on
+// the SMs slowed the running kernel, so those launch plainly.
+extern bool g_pdl_enabled;
+extern thread_local bool t_pdl_scope;
+constexpr int64_t kPdlLevelRows = 1 << 18;
+struct PdlScope {
+  bool old;
+  explicit PdlScope(bool on) : old(t_pdl_scope) { t_pdl_scope = on; }
+  ~PdlScope() { t_pdl_scope = old; }
+};
+template <class... KArgs, class... Args>
+inline cudaError_t launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = g_pdl_enabled && t_pdl_scope ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...);
+}
+
+#define FG_LAUNCH_PDL(kernel, grid, block, smem, stream, ...)                                  \
+  do {                                                                                         \
+    ::femgpu::g_kernel_launches.fetch_add(1, std::memory_order_relaxed);                       \
+    FG_CUDA(::femgpu::launch_pdl((kernel), dim3(grid), dim3(block), (smem), (stream), __VA_ARGS__)); \
+  } while (0)
+
 struct Mesh {
   int dim = 0, k = 0;
   int64_t nv = 0, ne = 0;
