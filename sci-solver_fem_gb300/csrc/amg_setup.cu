@@ -1619,33 +1619,56 @@ __global__ void spgemm_dense_warp_kernel(EscArgs<T> a, int ncols, const int32_t*
   for (int k = lane; k < ncols; k += 32) mark[k] = 0;
   __syncwarp();
   const unsigned below = (1u << lane) - 1u;
+  // adds product v to column col (lanes hold distinct columns within one right row)
+  int nt = 0;
+  auto add = [&](bool live, int col, T v) {
+    const bool fresh = live && mark[col] == 0;
+    if (fresh) {
+      mark[col] = 1;
+      acc[col] = v;
+    } else if (live) {
+      acc[col] = acc[col] + v;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, fresh);
+    if (fresh) list[nt + __popc(m & below)] = col;
+    nt += __popc(m);
+  };
   for (int i = blockIdx.x * nw + w; i < a.n; i += gridDim.x * nw) {
-    int nt = 0;
-    const int q1 = a.arp[i + 1];
-    for (int q = a.arp[i]; q < q1; q++) {
-      const int j = a.aci[q];
-      const T av = a.av[q];
-      const int b1 = a.brp[j + 1];
-      for (int f0 = a.brp[j]; f0 < b1; f0 += 32) {
-        const int f = f0 + lane;
-        const bool live = f < b1;
-        int col = 0;
-        T v = (T)0;
-        if (live) {
-          col = a.bci[f];
-          v = av * a.bv[f];
+    nt = 0;
+    const int qb = a.arp[i], qe = a.arp[i + 1];
+    // the left row in chunks of 32 entries: lane t holds entry q0 + t's value and right
+    // row bounds; each right row's first 32 entries are loaded one entry ahead
+    for (int q0 = qb; q0 < qe; q0 += 32) {
+      const int nq = min(32, qe - q0);
+      T avq = (T)0;
+      int bs = 0, be = 0;
+      if (lane < nq) {
+        const int j = a.aci[q0 + lane];
+        avq = a.av[q0 + lane];
+        bs = a.brp[j];
+        be = a.brp[j + 1];
+      }
+      int b0 = __shfl_sync(0xffffffffu, bs, 0), b1 = __shfl_sync(0xffffffffu, be, 0);
+      int ncol = b0 + lane < b1 ? a.bci[b0 + lane] : 0;
+      T nval = b0 + lane < b1 ? a.bv[b0 + lane] : (T)0;
+      for (int u = 0; u < nq; u++) {
+        const T av = __shfl_sync(0xffffffffu, avq, u);
+        const int c0 = ncol;
+        const T v0 = nval;
+        const int cb0 = b0, cb1 = b1;
+        if (u + 1 < nq) {
+          b0 = __shfl_sync(0xffffffffu, bs, u + 1);
+          b1 = __shfl_sync(0xffffffffu, be, u + 1);
+          ncol = b0 + lane < b1 ? a.bci[b0 + lane] : 0;
+          nval = b0 + lane < b1 ? a.bv[b0 + lane] : (T)0;
         }
-        const bool fresh = live && mark[col] == 0;
-        if (fresh) {
-          mark[col] = 1;
-          acc[col] = v;
-        } else if (live) {
-          acc[col] = acc[col] + v;
-        }
-        const unsigned m = __ballot_sync(0xffffffffu, fresh);
-        if (fresh) list[nt + __popc(m & below)] = col;
-        nt += __popc(m);
+        add(cb0 + lane < cb1, c0, av * v0);
         __syncwarp();
+        for (int f = cb0 + 32 + lane; f - lane < cb1; f += 32) {
+          const bool live = f < cb1;
+          add(live, live ? a.bci[f] : 0, live ? av * a.bv[f] : (T)0);
+          __syncwarp();
+        }
       }
     }
     const int np2 = next_pow2(nt < 2 ? 2 : nt);

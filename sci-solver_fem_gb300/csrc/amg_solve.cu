@@ -465,9 +465,6 @@ __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
   if (t == 0) {
     mbar_init(bar, 1);
     mbar_init(bar + 1, 1);
-    // zero slot of both x buffers (slot kRegGroupRows of copy 0)
-    xa[kRegGroupRows] = (T)0;
-    xb[kRegGroupRows] = (T)0;
     if (g0 < ngroups) {
       const int es0 = irp[rs];
       sh_es[0] = es0;
@@ -572,9 +569,8 @@ __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
     }
     const int kmax = __shfl_sync(0xffffffffu, len, 0);  // lane 0 holds the block's longest row
     const bool ok = mbar_wait_bounded(bar + buf, parity, wait_limit);
-    // Entry k of this lane's row: its value, and the byte offset of the x it reads within
-    // an x buffer (column + copy stride, times sizeof(T): below 2^16), two per register.
-    // Entries past the row's end hold value 0 and the offset of the zero slot.
+    // Entry k of this lane's row: its value, and the index of the x it reads within an x
+    // buffer (group-local column + copy stride: below 2^16), two per register.
     T val[K];
     uint32_t offp[K / 2];
     {
@@ -590,7 +586,7 @@ __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
         const unsigned m = __ballot_sync(0xffffffffu, k < len);
         const bool a = ok && k < len;
         val[k] = a ? sval[dk] : (T)0;
-        const uint32_t o = (a ? (uint32_t)scol[dk] : (uint32_t)kRegGroupRows) * (uint32_t)sizeof(T);
+        const uint32_t o = a ? (uint32_t)scol[dk] : 0u;
         if (k & 1) offp[k >> 1] |= o << 16;
         else offp[k >> 1] = o;
         dk += __popc(m);
@@ -615,23 +611,13 @@ __global__ void __launch_bounds__(512, 2) smooth_reg_kernel(
       }
       return;
     }
-    // Fused multiply-adds in entry order, four entries per step while the block's longest
-    // row has entries left (a branch the whole warp takes alike).  An entry past the row's
-    // end adds 0 * 0 to the sum, which leaves it unchanged: the sum starts at +0 and an
-    // exact cancellation rounds to +0, so it is never -0.
+    // Fused multiply-adds in entry order over the row's entries (lanes past their row's
+    // end are predicated off and touch no shared memory).
     auto rowsum = [&](const T* src) {
-      const unsigned char* srcb = reinterpret_cast<const unsigned char*>(src);
       T sax = 0;
 #pragma unroll
-      for (int k0 = 0; k0 < K; k0 += 4) {
-        if (k0 < kmax) {
-#pragma unroll
-          for (int k = k0; k < k0 + 4; k++) {
-            const uint32_t o = (k & 1) ? offp[k >> 1] >> 16 : offp[k >> 1] & 0xffffu;
-            sax = fma(val[k], *reinterpret_cast<const T*>(srcb + o), sax);
-          }
-        }
-      }
+      for (int k = 0; k < K; k++)
+        if (k < kmax && k < len) sax = fma(val[k], src[(offp[k >> 1] >> ((k & 1) * 16)) & 0xffffu], sax);
       return sax;
     };
     auto sweep = [&](const T* src, T* dst) {
