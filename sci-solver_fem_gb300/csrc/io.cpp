@@ -87,6 +87,9 @@ femgpu_status read_tetgen(const char* node, const char* ele, TetFile& out) {
 }
 
 // PLY (ascii, binary_little_endian): vertex x/y/z and polygon faces (fan-split).
+// Coordinates are kept in double as parsed: the reference's TriMesh reader scans ASCII
+// values with "%lf" into its double vertices (src/core/aggmis/cuda/TriMesh_io.cu,
+// read_verts_asc), and binary values keep their stored precision.
 struct PlyProp {
   std::string name, type, count_type;
   bool list = false;
@@ -183,9 +186,9 @@ femgpu_status read_ply(const char* file, std::vector<double>& xyz, std::vector<i
           } else {
             double v;
             if (!(ss >> v)) return FEMGPU_ERR_IO;
-            if (is_v && p.name == "x") pos[0] = (float)v;
-            if (is_v && p.name == "y") pos[1] = (float)v;
-            if (is_v && p.name == "z") pos[2] = (float)v;
+            if (is_v && p.name == "x") pos[0] = v;
+            if (is_v && p.name == "y") pos[1] = v;
+            if (is_v && p.name == "z") pos[2] = v;
           }
         }
       } else {
@@ -203,9 +206,9 @@ femgpu_status read_ply(const char* file, std::vector<double>& xyz, std::vector<i
             int sz = type_size(p.type);
             if (!sz || !in.read((char*)buf, sz)) return FEMGPU_ERR_IO;
             double v = read_bin(buf, p.type);
-            if (is_v && p.name == "x") pos[0] = (float)v;
-            if (is_v && p.name == "y") pos[1] = (float)v;
-            if (is_v && p.name == "z") pos[2] = (float)v;
+            if (is_v && p.name == "x") pos[0] = v;
+            if (is_v && p.name == "y") pos[1] = v;
+            if (is_v && p.name == "z") pos[2] = v;
           }
         }
       }

@@ -1,11 +1,13 @@
-"""Pins the mesh reader and the sparsity pattern to the reference's own code (no GPU).
+"""Pins the mesh readers and the sparsity patterns to the reference's own code (no GPU).
 
 The reference's TetMesh reader and vertex-neighbour builder (src/core/cuda/tetmesh.cu,
-TetMesh::read :251-376 and need_neighbors :112-170) have no CUSP dependency, so
-oracle/ref.mk compiles them from the reference sources into oracle/_ref/.  The pattern
-the reference builds from them (tetmesh2ell, src/core/cuda/cutil.cu:169-230) is row i =
-[i, sorted neighbours of i]; this repository stores the same columns in ascending order.
-Skipped where the reference checkout is absent (the library is built from its sources).
+TetMesh::read :251-376 and need_neighbors :112-170) and its TriMesh PLY reader and
+neighbour builder (src/core/aggmis/cuda/TriMesh_io.cu, TriMesh_connectivity.cu) have no
+CUSP dependency, so oracle/ref.mk compiles them from the reference sources into
+oracle/_ref/.  The pattern the reference builds from them (tetmesh2ell and trimesh2ell,
+src/core/cuda/cutil.cu:169-230,297-348) is row i = [i, sorted neighbours of i]; this
+repository stores the same columns in ascending order.  Skipped where the reference
+checkout is absent (the library is built from its sources).
 """
 import ctypes as C
 import os
@@ -34,6 +36,10 @@ def ref():
     L.ref_tetmesh_arrays.argtypes = [C.c_void_p, C.c_void_p]
     L.ref_tetmesh_neighbors.argtypes = [C.c_void_p, C.c_void_p]
     L.ref_tetmesh_neighbors.restype = C.c_int64
+    L.ref_trimesh_read.argtypes = [C.c_char_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+    L.ref_trimesh_arrays.argtypes = [C.c_void_p, C.c_void_p]
+    L.ref_trimesh_neighbors.argtypes = [C.c_void_p, C.c_void_p]
+    L.ref_trimesh_neighbors.restype = C.c_int64
     return L
 
 
@@ -90,3 +96,44 @@ def test_reader_and_pattern_match_the_reference(ref, tmp_path_factory, ref_data)
         for i in range(xyz.shape[0]):
             row = nbr[off[i]:off[i + 1]]
             assert len(np.unique(row)) == len(row), (base, i)
+
+
+def reference_trimesh(L, path):
+    nv, nf = C.c_int64(), C.c_int64()
+    assert L.ref_trimesh_read(path.encode(), C.byref(nv), C.byref(nf)) == 0
+    xyz = np.zeros((nv.value, 3))
+    faces = np.zeros((nf.value, 3), np.int32)
+    L.ref_trimesh_arrays(xyz.ctypes.data, faces.ctypes.data)
+    off = np.zeros(nv.value + 1, np.int32)
+    total = L.ref_trimesh_neighbors(off.ctypes.data, None)
+    nbr = np.zeros(max(total, 1), np.int32)
+    L.ref_trimesh_neighbors(off.ctypes.data, nbr.ctypes.data)
+    return xyz, faces, off, nbr[:total]
+
+
+def write_ply(path, xyz, faces):
+    with open(path, "w") as f:
+        f.write("ply\nformat ascii 1.0\n")
+        f.write(f"element vertex {xyz.shape[0]}\nproperty float x\nproperty float y\nproperty float z\n")
+        f.write(f"element face {faces.shape[0]}\nproperty list uchar int vertex_indices\nend_header\n")
+        for p in xyz:
+            f.write(f"{p[0]:.7g} {p[1]:.7g} {p[2]:.7g}\n")
+        for t in faces:
+            f.write(f"3 {t[0]} {t[1]} {t[2]}\n")
+
+
+def test_ply_reader_and_pattern_match_the_reference(ref, tmp_path, ref_data):
+    xyz2, tri2 = meshes.jittered_square(24, seed=5)
+    xyz3 = np.zeros((xyz2.shape[0], 3))
+    xyz3[:, : xyz2.shape[1]] = xyz2[:, :3] if xyz2.shape[1] >= 3 else xyz2
+    write_ply(str(tmp_path / "square24.ply"), xyz3, tri2)
+    for path in (os.path.join(ref_data, "simple.ply"), os.path.join(ref_data, "sphere_290verts.ply"),
+                 str(tmp_path / "square24.ply")):
+        rxyz, rfaces, off, nbr = reference_trimesh(ref, path)
+        xyz, conn = femgpu.read_ply(path)
+        assert np.array_equal(xyz, rxyz), path
+        assert np.array_equal(conn, rfaces), path
+        rp, ci = O.build_pattern(xyz.shape[0], conn)
+        for i in range(xyz.shape[0]):
+            want = np.unique(np.concatenate([[i], nbr[off[i]:off[i + 1]]]))
+            assert np.array_equal(ci[rp[i]:rp[i + 1]], want), (path, i)
