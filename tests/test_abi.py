@@ -114,3 +114,29 @@ def test_corrupt_files_return_io_status(tmp_path):
     assert e.value.status == 7
     with pytest.raises(femgpu.FemgpuError):
         femgpu.read_ply(str(tmp_path / "missing.ply"))
+
+
+def test_ply_coordinates_keep_their_stored_precision(tmp_path):
+    # ASCII values are scanned as double (the reference's TriMesh reader uses "%lf");
+    # binary float and double properties keep their stored values
+    xyz = np.array([[0.1, 0.2, 0.0], [1.0 / 3.0, 0.7, 0.0], [0.9, 0.123456789012345, 0.0]])
+    faces = np.array([[0, 1, 2]], np.int32)
+    asc = tmp_path / "a.ply"
+    with open(asc, "w") as f:
+        f.write("ply\nformat ascii 1.0\nelement vertex 3\nproperty double x\nproperty double y\n"
+                "property double z\nelement face 1\nproperty list uchar int vertex_indices\nend_header\n")
+        for p in xyz:
+            f.write(" ".join(repr(float(c)) for c in p) + "\n")
+        f.write("3 0 1 2\n")
+    got, tri = femgpu.read_ply(str(asc))
+    assert np.array_equal(got, xyz) and np.array_equal(tri, faces)
+    for typ, dt in (("double", "<f8"), ("float", "<f4")):
+        b = tmp_path / f"b_{typ}.ply"
+        with open(b, "wb") as f:
+            f.write((f"ply\nformat binary_little_endian 1.0\nelement vertex 3\nproperty {typ} x\n"
+                     f"property {typ} y\nproperty {typ} z\nelement face 1\n"
+                     "property list uchar int vertex_indices\nend_header\n").encode())
+            f.write(xyz.astype(dt).tobytes())
+            f.write(np.array([3], np.uint8).tobytes() + faces.astype("<i4").tobytes())
+        got, tri = femgpu.read_ply(str(b))
+        assert np.array_equal(got, xyz.astype(dt).astype(np.float64)) and np.array_equal(tri, faces)
