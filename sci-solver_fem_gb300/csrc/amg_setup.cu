@@ -2274,6 +2274,7 @@ void build_levels(Ctx& c, Hierarchy<T>& H) {
       break;
     }
     PhaseTimer pt(s, num_levels - 1);
+    const TraceRange level_range("femgpu setup: level");
     OldMisOut o;
     old_mis(c, N, L.gxadj.p, L.gadj.p, o);
     pt.mark("aggregate");

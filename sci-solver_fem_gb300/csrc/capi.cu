@@ -28,8 +28,11 @@ struct PoolScope {
   ~PoolScope() { g_alloc_pool = saved; }
 };
 
-femgpu_status guard(femgpu_handle h, const std::function<void()>& fn) {
+// Runs fn for an entry point: the handle's memory pool and device, exceptions turned into
+// status codes, and (with a name) an NVTX range around the call.
+femgpu_status guard(femgpu_handle h, const std::function<void()>& fn, const char* trace = nullptr) {
   PoolScope scope(h);
+  TraceRange range(trace);
   try {
     if (h) FG_CUDA(cudaSetDevice(h->device));
     fn();
@@ -324,7 +327,7 @@ femgpu_status femgpu_assemble(femgpu_handle h, const double* coef, double lambda
     h->assembled_from_mesh = true;
     h->dmask.release();
     FG_CUDA(cudaStreamSynchronize(h->stream));
-  });
+  }, "femgpu_assemble");
 }
 
 femgpu_status femgpu_assemble_device(femgpu_handle h, const double* d_coef, double lambda_mass) {
@@ -337,7 +340,7 @@ femgpu_status femgpu_assemble_device(femgpu_handle h, const double* d_coef, doub
     h->assembled_from_mesh = true;
     h->dmask.release();
     FG_CUDA(cudaStreamSynchronize(h->stream));
-  });
+  }, "femgpu_assemble_device");
 }
 
 femgpu_status femgpu_load_vector(femgpu_handle h, const double* f, double* b) {
@@ -391,17 +394,17 @@ femgpu_status femgpu_set_matrix_csr(femgpu_handle h, int64_t n, const int32_t* r
 
 femgpu_status femgpu_setup(femgpu_handle h) {
   if (!h) return FEMGPU_ERR_INVALID;
-  return guard(h, [&] { amg_setup(*h); });
+  return guard(h, [&] { amg_setup(*h); }, "femgpu_setup");
 }
 
 femgpu_status femgpu_save_hierarchy(femgpu_handle h, const char* path) {
   if (!h || !path) return FEMGPU_ERR_INVALID;
-  return guard(h, [&] { save_hierarchy(*h, path); });
+  return guard(h, [&] { save_hierarchy(*h, path); }, "femgpu_save_hierarchy");
 }
 
 femgpu_status femgpu_load_hierarchy(femgpu_handle h, const char* path) {
   if (!h || !path) return FEMGPU_ERR_INVALID;
-  return guard(h, [&] { load_hierarchy(*h, path); });
+  return guard(h, [&] { load_hierarchy(*h, path); }, "femgpu_load_hierarchy");
 }
 
 femgpu_status femgpu_solve_device(femgpu_handle h, const double* d_b, double* d_x, femgpu_solve_stats* stats) {
@@ -430,7 +433,7 @@ femgpu_status femgpu_solve_device(femgpu_handle h, const double* d_b, double* d_
     result = r.status;
     if (r.status == FEMGPU_ERR_NOT_CONVERGED) h->last_error = "PCG reached maxIters";
     if (r.status == FEMGPU_ERR_BREAKDOWN) h->last_error = "PCG breakdown (non-positive curvature or NaN)";
-  });
+  }, "femgpu_solve_device");
   return st != FEMGPU_OK ? st : result;
 }
 
@@ -446,7 +449,7 @@ femgpu_status femgpu_solve(femgpu_handle h, const double* b, double* x, femgpu_s
     result = femgpu_solve_device(h, db.p, dx.p, stats);
     dx.download(x, n);
     FG_CUDA(cudaStreamSynchronize(h->stream));
-  });
+  }, "femgpu_solve");
   return st != FEMGPU_OK ? st : result;
 }
 
@@ -500,7 +503,7 @@ femgpu_status femgpu_solve_multi_device(femgpu_handle h, int nrhs, const double*
     }
     if (result == FEMGPU_ERR_NOT_CONVERGED) h->last_error = "PCG reached maxIters on a right-hand side";
     if (result == FEMGPU_ERR_BREAKDOWN) h->last_error = "PCG breakdown on a right-hand side";
-  });
+  }, "femgpu_solve_multi_device");
   return st != FEMGPU_OK ? st : result;
 }
 
@@ -525,6 +528,7 @@ femgpu_status femgpu_solve_batch(int count, femgpu_handle* hs, const double* con
                                  int threads, femgpu_solve_stats* stats) {
   if (count < 0 || threads < 0) return FEMGPU_ERR_INVALID;
   if (count == 0) return FEMGPU_OK;
+  const TraceRange range("femgpu_solve_batch");
   if (!hs || !b || !x) return FEMGPU_ERR_INVALID;
   std::vector<femgpu_handle> seen(hs, hs + count);
   for (int i = 0; i < count; i++)
@@ -641,7 +645,7 @@ femgpu_status femgpu_adjoint_grad_device(femgpu_handle h, const double* d_dLdu, 
     result = r.status;
     if (r.status == FEMGPU_ERR_NOT_CONVERGED) h->last_error = "adjoint PCG reached maxIters";
     if (r.status == FEMGPU_ERR_BREAKDOWN) h->last_error = "adjoint PCG breakdown (non-positive curvature or NaN)";
-  });
+  }, "femgpu_adjoint_grad_device");
   return st != FEMGPU_OK ? st : result;
 }
 
@@ -721,7 +725,7 @@ femgpu_status femgpu_vcycle(femgpu_handle h, const double* r, double* z) {
     amg_vcycle_device(*h, dr.p, dz.p);
     dz.download(z, n);
     FG_CUDA(cudaStreamSynchronize(h->stream));
-  });
+  }, "femgpu_vcycle");
 }
 
 femgpu_status femgpu_profile_kernel(femgpu_handle h, int which, int reps, double* avg_ms, double* bytes) {

@@ -10,6 +10,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 #include <atomic>
@@ -22,6 +23,21 @@
 #include "../../include/femgpu.h"
 
 namespace femgpu {
+
+// A named NVTX range over a scope: Nsight Systems and Nsight Compute show the library's
+// calls and setup levels on the timeline when they run the program; without a tool
+// attached the push and pop do nothing.  A null name opens no range.
+struct TraceRange {
+  bool on;
+  explicit TraceRange(const char* name) : on(name != nullptr) {
+    if (on) nvtxRangePushA(name);
+  }
+  ~TraceRange() {
+    if (on) nvtxRangePop();
+  }
+  TraceRange(const TraceRange&) = delete;
+  TraceRange& operator=(const TraceRange&) = delete;
+};
 
 struct Error : std::runtime_error {
   femgpu_status status;
